@@ -1,0 +1,76 @@
+/*
+ * polgraw_gb300_host.h -- host side of the drop-in search program
+ * (gwsearch-gb300), exported by libpolgraw_gb300.so.
+ *
+ * It re-implements, in this project's own C, the set-up and sky loop of the
+ * reference network search that surround job_core():
+ *   handle_opts        search/network/src-cpu/init.c:28-281
+ *   read_grid          init.c:287-321
+ *   search_settings    settings.c:16-81
+ *   detectors_settings settings.c:92-246
+ *   init_arrays        init.c:326-457 (data, sig2, ephemerides)
+ *   narrow_down_band / read_lines / lines_in_band / fraction_of_band_vetoed
+ *                      settings.c:327-656
+ *   rogcvir            settings.c:253-275
+ *   add_signal         init.c:462-651
+ *   set_search_range   init.c:656-804 (+ gridr, auxi.c:143-212)
+ *   read_checkpoints   init.c:868-917
+ *   search             jobcore.c:51-184 (state file, trigger append)
+ *   main               main.c:37-155
+ * with the same command-line options, input files, trigger-file layout and
+ * state-file semantics.  Differences are listed in the function comments.
+ */
+#ifndef POLGRAW_GB300_HOST_H
+#define POLGRAW_GB300_HOST_H
+
+#include "polgraw_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pa_host pa_host;
+
+/* Exit-code-like results of the host steps. */
+enum {
+  PA_HOST_OK = 0,
+  PA_HOST_EXIT_SUCCESS = 100,  /* reference would exit(EXIT_SUCCESS) here */
+  PA_HOST_EXIT_FAILURE = 101   /* reference would exit(EXIT_FAILURE) here */
+};
+
+/* handle_opts(): parses argv (getopt_long_only, same option table) plus the
+ * GB300 options -precision {mixed|fp64}, -phase {f64|fixed|ff},
+ * -sbatch <spindowns per launch>, -skybatch <sky points per batch>,
+ * -device <ordinal>.  Returns NULL with *rc set on --help or bad input. */
+pa_host *pa_host_create(int argc, char **argv, int *rc);
+
+/* main.c:58-135: output directory, grid, settings, detectors, data,
+ * band narrowing and line veto, rogcvir, injection or range, -getrange,
+ * checkpoint.  Returns PA_HOST_OK, PA_HOST_EXIT_SUCCESS (nothing left to
+ * do: -getrange, fully vetoed band, empty state file) or
+ * PA_HOST_EXIT_FAILURE. */
+int pa_host_setup(pa_host *h);
+
+/* search() (jobcore.c:51-184) over the context: state file before each
+ * sky point, locked append of the candidate buffer when it holds more than
+ * nfft records and at the end of each hemisphere, state file emptied at the
+ * end (main.c:142-147).  Returns PA_HOST_OK or PA_HOST_EXIT_FAILURE. */
+int pa_host_search(pa_host *h, pa_ctx *ctx);
+
+/* Runs the whole program (gwsearch-gb300 main). */
+int pa_host_main(int argc, char **argv);
+
+void pa_host_destroy(pa_host *h);
+
+/* Accessors for tests and embedding callers. */
+const pa_settings *pa_host_settings(const pa_host *h);
+const pa_detector *pa_host_detectors(const pa_host *h, int *nifo);
+const pa_range *pa_host_range(const pa_host *h);
+void pa_host_core_opts(const pa_host *h, pa_opts *out);
+void pa_host_config(const pa_host *h, pa_config *out);
+const char *pa_host_detector_name(const pa_host *h, int i);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

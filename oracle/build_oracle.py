@@ -1,0 +1,119 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+Two things are built here:
+
+* ``oracle/_build/liboracle.so`` -- the all-FP64 C restatement of the
+  reference hot path (oracle.c + fft.c), OpenMP-parallel over spindowns.  It is
+  the parity checker for the CUDA library and the timed CPU baseline ("port")
+  of bench.py.  Built from this repository's sources on any machine.
+
+* ``oracle/_ref/`` -- the UNMODIFIED reference search compiled from its own
+  sources where they lie (search/network/src-cpu and src-openmp under the
+  reference checkout), linked against the FFTW3/GSL shims in ``oracle/shim``
+  because neither library is installed here.  Built only where the reference
+  checkout exists; nothing of it is committed (``oracle/_ref`` is
+  git-ignored).  Its outputs pin the oracle through the golden fixtures in
+  ``tests/golden``.
+
+Flags: ``-ffp-contract=off`` everywhere so that no FMA contraction changes
+roundings between x86-64 and aarch64 builds of the oracle; ``-fcommon``
+because the reference defines ``ifo[]`` in a header (struct.h:177);
+``-DGNUSINCOS`` selects glibc sincos (jobcore.c:528) instead of the
+prebuilt vector libraries.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+REFERENCE_ROOT = "/root/reference"
+NETWORK = os.path.join(REFERENCE_ROOT, "search", "network")
+
+ORACLE_LIB = os.path.join(BUILD, "liboracle.so")
+REF_SERIAL = os.path.join(REF_OUT, "gwsearch-ref")
+REF_OMP = os.path.join(REF_OUT, "gwsearch-ref-omp")
+
+_CC = os.environ.get("CC", "gcc")
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def _newer(target: str, sources: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build_oracle(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = [os.path.join(HERE, f) for f in ("oracle.c", "fft.c")]
+    deps = srcs + [os.path.join(HERE, f) for f in ("oracle.h", "fft.h")] + [
+        os.path.join(HERE, "..", "include", "polgraw_gb300.h")]
+    if force or _newer(ORACLE_LIB, deps):
+        tmp = ORACLE_LIB + ".tmp%d" % os.getpid()
+        _run([_CC, "-std=gnu11", "-O2", "-fPIC", "-shared", "-fopenmp",
+              "-ffp-contract=off", "-Wall", "-Wno-unused", "-o", tmp] + srcs + ["-lm"])
+        os.replace(tmp, ORACLE_LIB)
+    return ORACLE_LIB
+
+
+def reference_available() -> bool:
+    return os.path.isdir(os.path.join(NETWORK, "src-cpu"))
+
+
+def _build_ref_variant(subdir: str, out: str, extra: list[str]) -> str:
+    src_dir = os.path.join(NETWORK, subdir)
+    names = ["main.c", "jobcore.c", "timer.c", "settings.c", "auxi.c", "init.c"]
+    srcs = [os.path.join(src_dir, n) for n in names]
+    shims = [os.path.join(HERE, "shim", "fftw_shim.c"), os.path.join(HERE, "shim", "gsl_shim.c"),
+             os.path.join(HERE, "fft.c")]
+    if not _newer(out, srcs + shims):
+        return out
+    os.makedirs(REF_OUT, exist_ok=True)
+    objdir = os.path.join(REF_OUT, "obj_" + subdir)
+    os.makedirs(objdir, exist_ok=True)
+    cflags = ["-std=gnu11", "-fcommon", "-DGNUSINCOS", "-DPREFIX=./candidates",
+              "-DCODEVER=reference", "-I" + os.path.join(HERE, "shim"), "-w"] + extra
+    objs = []
+    for s in srcs + shims:
+        o = os.path.join(objdir, os.path.basename(s).replace(".c", ".o"))
+        inc = ["-I" + src_dir] if s in srcs else ["-I" + os.path.join(HERE, "shim")]
+        _run([_CC] + cflags + inc + ["-c", s, "-o", o])
+        objs.append(o)
+    _run([_CC] + [f for f in extra if f.startswith("-f")] + ["-o", out] + objs + ["-lm", "-lpthread"])
+    shutil.rmtree(objdir, ignore_errors=True)
+    return out
+
+
+def build_reference() -> dict:
+    """Compile the reference search (serial parity build and OpenMP timing
+    build).  Returns {} when the reference checkout is absent."""
+    if not reference_available():
+        return {}
+    out = {}
+    # parity build: no fast-math, verbose candidate lines, spindown timers.
+    # -fno-builtin: add_signal reads "snr"/"amp" into char amporsnr[3]
+    # (init.c:475,486), a one-byte overflow after which GCC folds
+    # strcmp(amporsnr, "snr") to "different" and the injection is refused;
+    # without the builtin the comparison behaves as the authors intended.
+    out["serial"] = _build_ref_variant(
+        "src-cpu", REF_SERIAL, ["-O2", "-ffp-contract=off", "-fno-builtin", "-DTIMERS=3", "-DVERBOSE"])
+    # timing build: the reference's own optimisation flags (src-openmp/Makefile)
+    out["omp"] = _build_ref_variant(
+        "src-openmp", REF_OMP, ["-O3", "-ffast-math", "-fopenmp", "-fno-builtin", "-DTIMERS=3"])
+    return out
+
+
+if __name__ == "__main__":
+    print(build_oracle(force="--force" in sys.argv))
+    print(build_reference())

@@ -1,0 +1,116 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker.  The product never uses it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import build_oracle  # noqa: E402
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = build_oracle.build_oracle()
+    lib = C.CDLL(path)
+    lib.ora_create.restype = C.c_void_p
+    lib.ora_create.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+    lib.ora_destroy.argtypes = [C.c_void_p]
+    lib.ora_destroy.restype = None
+    P = C.POINTER
+    lib.ora_job_core.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, P(C.c_int),
+                                 P(C.c_double), C.c_int, C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_double),
+                                 P(C.c_double), P(C.c_double), P(C.c_double), C.c_int, P(C.c_double)]
+    lib.ora_fft.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_double)]
+    lib.ora_search_settings.argtypes = [C.c_void_p]
+    lib.ora_search_settings.restype = None
+    lib.ora_spindown_range.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, P(C.c_int), P(C.c_int)]
+    _lib = lib
+    return lib
+
+
+class Oracle:
+    """All-FP64 CPU restatement of job_core() over the same pa_settings /
+    pa_detector inputs as the GPU context."""
+
+    def __init__(self, settings, dets, nifo: int, nthreads: int = 0):
+        self.lib = load()
+        self.settings = settings
+        self.nifo = nifo
+        self.o = self.lib.ora_create(C.addressof(settings), C.cast(dets, C.c_void_p), nifo, nthreads)
+        if not self.o:
+            raise RuntimeError("ora_create failed")
+
+    def job_core(self, pm, mm, nn, opts, rng, cap: int = 1 << 16, want_prelude=False, F_ss=None):
+        from importlib import import_module
+        pa_lib = import_module("polgraw_gb300.lib")
+        N = self.settings.N
+        sgnlc = C.c_int(0)
+        fnum = C.c_int(0)
+        needed = C.c_int(0)
+        PD = C.POINTER(C.c_double)
+        while True:
+            buf = np.zeros((cap, 5))
+            idx = (pa_lib.CandIdx * cap)()
+            pre_a = np.zeros((self.nifo, N), np.complex128) if want_prelude else None
+            pre_b = np.zeros((self.nifo, N), np.complex128) if want_prelude else None
+            aa = C.c_double(0)
+            bb = C.c_double(0)
+            Fo = np.zeros(self.settings.nmax - self.settings.nmin) if F_ss is not None else None
+            rc = self.lib.ora_job_core(
+                self.o, pm, mm, nn, C.addressof(opts), C.addressof(rng), C.byref(sgnlc),
+                buf.ctypes.data_as(PD), cap, C.addressof(idx), C.byref(fnum), C.byref(needed),
+                pre_a.ctypes.data_as(PD) if want_prelude else None,
+                pre_b.ctypes.data_as(PD) if want_prelude else None, C.byref(aa), C.byref(bb),
+                int(F_ss) if F_ss is not None else -(1 << 30),
+                Fo.ctypes.data_as(PD) if Fo is not None else None)
+            if rc == -1:
+                cap = needed.value + 16
+                continue
+            break
+        n = sgnlc.value
+        out = {"records": buf[:n].copy(), "idx": pa_lib.idx_to_array(idx, n), "FNum": fnum.value,
+               "aa": aa.value, "bb": bb.value}
+        if want_prelude:
+            out["pre_a"], out["pre_b"] = pre_a, pre_b
+        if Fo is not None:
+            out["F"] = Fo
+        return out
+
+    def job_core3(self, pm, mm, nn, opts, rng):
+        """(records, idx, FNum increment), the shape of lib.Context.job_core."""
+        d = self.job_core(pm, mm, nn, opts, rng)
+        return d["records"], d["idx"], d["FNum"]
+
+    def close(self):
+        if self.o:
+            self.lib.ora_destroy(self.o)
+            self.o = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fft(x: np.ndarray, sign: int) -> np.ndarray:
+    lib = load()
+    x = np.ascontiguousarray(x, dtype=np.complex128)
+    out = np.empty_like(x)
+    rc = lib.ora_fft(x.size, sign, x.ctypes.data_as(C.POINTER(C.c_double)),
+                     out.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc:
+        raise ValueError("length must be a power of two")
+    return out

@@ -1,0 +1,13 @@
+"""polgraw_gb300: GB300-native coherent F-statistic search (drop-in for the
+Polgraw all-sky network search's job_core hot path).
+
+The directory name contains a hyphen, so the package is registered under the
+import name ``polgraw_gb300`` by a path loader (see ``load_package`` in
+``bench.py``/``tests/conftest.py``).  Submodules:
+
+* ``lib``   -- ctypes binding of the C-ABI in include/polgraw_gb300.h
+* ``build`` -- nvcc/gcc recipes for libpolgraw_gb300.so and the C host
+* ``synth`` -- synthetic inputs in the reference's on-disk layout
+* ``host``  -- Python mirror of the reference host set-up (settings, data
+               reading, injection, ranges) used by tests and the bench
+"""

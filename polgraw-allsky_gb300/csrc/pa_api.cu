@@ -1,0 +1,654 @@
+// pa_api.cu -- the C-ABI of libpolgraw_gb300.so (include/polgraw_gb300.h).
+//
+// Host logic of job_core() around the device engine: sky-point scalars
+// (jobcore.c:243-299), spindown range (jobcore.c:424-444), candidate
+// records and the line veto (jobcore.c:670-687).  All FP64 host arithmetic
+// follows the reference expressions so that for the same (ss, ii) the
+// f, s1, delta, alpha fields of a record are bit-identical to the
+// reference's; this file is compiled with -ffp-contract=off for that.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/polgraw_gb300.h"
+#include "pa_engine.h"
+
+#define SQR(x) ((x) * (x))
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct Twiddles {
+  void* p[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+}  // namespace
+
+struct pa_ctx {
+  pa_settings sett;
+  std::vector<double> lines;
+  int nifo = 0;
+  pa_config cfg;
+  bool fp64 = false;
+  size_t rsz = 4;  // bytes of the Real type
+  pa::DetConst dc[pa::kMaxDet];
+  double det0[pa::kMaxDet][3];  // DetSSB of sample 0 (shft1)
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  pa::Buffers b;
+  std::vector<void*> allocs;
+  Twiddles tw_fwd, tw_inv, tw_main;
+  pa::Engine* eng = nullptr;
+  pa::DevCand* h_cand = nullptr;  // pinned
+  int* h_ncand = nullptr;          // pinned
+  std::string err;
+  long long extra_launches = 0;
+};
+
+static int fail(pa_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  else g_create_error = buf;
+  return code;
+}
+
+static int cuda_fail(pa_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, PA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                               \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+static int dalloc(pa_ctx* c, void** p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+  c->allocs.push_back(*p);
+  return PA_OK;
+}
+
+// exp(sign 2 pi i m / n) in FP64 with the angle folded to the first octant
+static void host_twiddle(long m, long n, int sign, double* re, double* im) {
+  long m8 = 8 * (m % n);
+  long oct = m8 / n, rem = m8 - oct * n;
+  double a = (oct & 1) ? (double)(n - rem) / (double)n * (M_PI / 4.0) : (double)rem / (double)n * (M_PI / 4.0);
+  double ca = cos(a), sa = sin(a), co, si;
+  switch (oct) {
+    case 0: co = ca; si = sa; break;
+    case 1: co = sa; si = ca; break;
+    case 2: co = -sa; si = ca; break;
+    case 3: co = -ca; si = sa; break;
+    case 4: co = -ca; si = -sa; break;
+    case 5: co = -sa; si = -ca; break;
+    case 6: co = sa; si = -ca; break;
+    default: co = ca; si = -sa; break;
+  }
+  *re = co;
+  *im = sign * si;
+}
+
+static int upload_real(pa_ctx* c, void* dst, const std::vector<double>& v) {
+  if (c->fp64) {
+    CK(cudaMemcpy(dst, v.data(), v.size() * 8, cudaMemcpyHostToDevice), "upload");
+  } else {
+    std::vector<float> f(v.size());
+    for (size_t i = 0; i < v.size(); i++) f[i] = (float)v[i];
+    CK(cudaMemcpy(dst, f.data(), f.size() * 4, cudaMemcpyHostToDevice), "upload");
+  }
+  return PA_OK;
+}
+
+// tw1 (L1), tw2 (L2), twlo (1024), twhi (L/1024) for length L and sign
+static int make_twiddles(pa_ctx* c, int L, int sign, Twiddles* t) {
+  int m = 0;
+  while ((1 << m) < L) ++m;
+  const int L1 = 1 << ((m + 1) / 2), L2 = 1 << (m / 2);
+  const int lens[4] = {L1, L2, 1024, L / 1024};
+  for (int k = 0; k < 4; k++) {
+    std::vector<double> v(2 * (size_t)lens[k]);
+    for (int j = 0; j < lens[k]; j++) {
+      long num, den;
+      if (k == 0) { num = j; den = L1; }
+      else if (k == 1) { num = j; den = L2; }
+      else if (k == 2) { num = j; den = L; }
+      else { num = (long)j * 1024; den = L; }
+      host_twiddle(num, den, sign, &v[2 * j], &v[2 * j + 1]);
+    }
+    int rc = dalloc(c, &t->p[k], v.size() * c->rsz);
+    if (rc) return rc;
+    rc = upload_real(c, t->p[k], v);
+    if (rc) return rc;
+  }
+  return PA_OK;
+}
+
+static void set_det_consts(pa_ctx* c, const pa_detector* det) {
+  for (int n = 0; n < c->nifo; n++) {
+    pa::DetConst& d = c->dc[n];
+    memcpy(d.amod, det[n].amod, sizeof(d.amod));
+    d.sig2 = det[n].sig2;
+    d.inv_sig2 = 1.0 / det[n].sig2;
+    d.sphir = det[n].sphir;
+    d.cphir = det[n].cphir;
+    for (int k = 0; k < 3; k++) c->det0[n][k] = det[n].DetSSB[k];
+  }
+}
+
+static int upload_data(pa_ctx* c, const pa_detector* det) {
+  const int N = c->sett.N;
+  for (int n = 0; n < c->nifo; n++) {
+    CK(cudaMemcpyAsync((double*)c->b.xDat + (size_t)n * N, det[n].xDat, sizeof(double) * N,
+                       cudaMemcpyHostToDevice, c->stream), "upload xDat");
+    CK(cudaMemcpyAsync((double*)c->b.DetSSB + (size_t)n * 3 * N, det[n].DetSSB, sizeof(double) * 3 * N,
+                       cudaMemcpyHostToDevice, c->stream), "upload DetSSB");
+  }
+  set_det_consts(c, det);
+  CK(cudaMemcpyAsync((void*)c->b.dc, c->dc, sizeof(pa::DetConst) * c->nifo, cudaMemcpyHostToDevice,
+                     c->stream), "upload detector constants");
+  CK(cudaStreamSynchronize(c->stream), "upload sync");
+  return PA_OK;
+}
+
+static int validate(const pa_settings* s, int nifo, const pa_config* cfg, char* why, size_t n) {
+  auto ispow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
+  if (nifo < 1 || nifo > PA_MAX_DETECTORS) return snprintf(why, n, "nifo=%d outside [1,%d]", nifo, PA_MAX_DETECTORS), 1;
+  if (s->N < 2) return snprintf(why, n, "N=%d too small", s->N), 1;
+  if (!ispow2(s->nfft) || s->nfft < 4096 || s->nfft > (1 << 19))
+    return snprintf(why, n, "nfft=%d must be a power of two in [4096, 2^19]", s->nfft), 1;
+  if (s->nfft < s->N) return snprintf(why, n, "nfft=%d < N=%d", s->nfft, s->N), 1;
+  if (s->interpftpad != 2) return snprintf(why, n, "interpftpad=%d (only 2 is supported, as in settings.c:56)", s->interpftpad), 1;
+  if (s->Ninterp != s->interpftpad * s->nfft) return snprintf(why, n, "Ninterp != interpftpad*nfft"), 1;
+  if (s->fftpad < 1 || s->nfftf != s->fftpad * s->nfft || !ispow2(s->nfftf) || s->nfftf > (1 << 20))
+    return snprintf(why, n, "nfftf=%d must be fftpad*nfft, a power of two <= 2^20", s->nfftf), 1;
+  if (s->nmin < 0 || s->nmax > s->nfftf || s->nmax <= s->nmin)
+    return snprintf(why, n, "bad F-statistic range [%d, %d)", s->nmin, s->nmax), 1;
+  if (s->numlines_band < 0 || s->numlines_band > PA_MAXL || (s->numlines_band && !s->lines))
+    return snprintf(why, n, "bad veto line list"), 1;
+  if (cfg && (cfg->precision < 0 || cfg->precision > 1 || cfg->phase_mode < 0 || cfg->phase_mode > 2))
+    return snprintf(why, n, "bad precision/phase_mode"), 1;
+  if (cfg && (cfg->spindown_batch < 0 || cfg->spindown_batch > 4096))
+    return snprintf(why, n, "spindown_batch outside [0, 4096]"), 1;
+  return 0;
+}
+
+static int build_ctx(pa_ctx* c, const pa_detector* det) {
+  const pa_settings& s = c->sett;
+  const int N = s.N, nifo = c->nifo;
+  CK(cudaSetDevice(c->dev), "cudaSetDevice");
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  pa::Buffers& b = c->b;
+  memset(&b, 0, sizeof(b));
+  b.N = N;
+  b.nfft = s.nfft;
+  b.Ninterp = s.Ninterp;
+  b.nfftf = s.nfftf;
+  b.nmin = s.nmin;
+  b.nmax = s.nmax;
+  b.bins = s.nmax - s.nmin;
+  b.nblk = b.bins / PA_NAVFSTAT;
+  b.nifo = nifo;
+  b.fftpad = s.fftpad;
+  int sb = c->cfg.spindown_batch;
+  if (sb <= 0) {
+    // keep the FFT intermediate of one batch near 64 MB (L2-sized)
+    const size_t per = 2 * (size_t)s.nfftf * 2 * c->rsz;
+    sb = (int)std::max<size_t>(1, std::min<size_t>(64, ((size_t)64 << 20) / per));
+  }
+  b.sbatch = sb;
+  const size_t rs = c->rsz, cs = 2 * c->rsz;
+  int rc;
+#define ALLOC(ptr, bytes)                              \
+  do {                                                 \
+    void* p_;                                          \
+    if ((rc = dalloc(c, &p_, (bytes)))) return rc;     \
+    ptr = decltype(ptr)(p_);                           \
+  } while (0)
+  ALLOC(b.xDat, sizeof(double) * nifo * (size_t)N);
+  ALLOC(b.DetSSB, sizeof(double) * nifo * 3 * (size_t)N);
+  ALLOC(b.cosmodf, rs * N);
+  ALLOC(b.sinmodf, rs * N);
+  ALLOC(b.dc, sizeof(pa::DetConst) * pa::kMaxDet);
+  ALLOC(b.spline_invp, sizeof(double) * 64);
+  ALLOC(b.spline_p, sizeof(double) * 64);
+  ALLOC(b.xin, cs * nifo * 2 * (size_t)N);
+  ALLOC(b.spec, cs * nifo * 2 * (size_t)s.nfft);
+  ALLOC(b.yint, cs * nifo * 2 * (size_t)s.Ninterp);
+  ALLOC(b.u, sizeof(double) * 2 * nifo * 2 * (size_t)(2 * N));
+  ALLOC(b.y2, cs * nifo * 2 * (size_t)(2 * N));
+  ALLOC(b.shftf, sizeof(double) * nifo * (size_t)N);
+  ALLOC(b.ph0, 8 * nifo * (size_t)N);
+  ALLOC(b.ph1, 8 * nifo * (size_t)N);
+  ALLOC(b.xm, cs * nifo * 2 * (size_t)N);
+  ALLOC(b.part, sizeof(double) * 2 * nifo * (size_t)((N + 255) / 256));
+  ALLOC(b.sums, sizeof(double) * 8);
+  const size_t ybytes = std::max((size_t)sb * 2 * s.nfftf, (size_t)nifo * 2 * s.Ninterp) * cs;
+  ALLOC(b.ybuf, ybytes);
+  ALLOC(b.F, rs * (size_t)sb * b.bins);
+  ALLOC(b.mu, rs * (size_t)sb * (b.nblk > 0 ? b.nblk : 1));
+  b.cand_cap = 1 << 18;
+  ALLOC(b.cand, sizeof(pa::DevCand) * (size_t)b.cand_cap);
+  ALLOC(b.ncand, sizeof(int) * 4);
+#undef ALLOC
+  CK(cudaMallocHost((void**)&c->h_cand, sizeof(pa::DevCand) * (size_t)b.cand_cap), "cudaMallocHost");
+  CK(cudaMallocHost((void**)&c->h_ncand, sizeof(int) * 4), "cudaMallocHost");
+  // constant tables
+  std::vector<double> cm(N), sm(N);
+  for (int i = 0; i < N; i++) {
+    double omrt = s.omr * i;  // init.c:450-455
+    cm[i] = cos(omrt);
+    sm[i] = sin(omrt);
+  }
+  if ((rc = upload_real(c, (void*)b.cosmodf, cm))) return rc;
+  if ((rc = upload_real(c, (void*)b.sinmodf, sm))) return rc;
+  double invp[64], p[64];
+  p[0] = 0.;
+  invp[0] = 0.;
+  for (int i = 1; i < 64; i++) {  // auxi.c:71-72
+    invp[i] = 2. / (p[i - 1] + 4.);
+    p[i] = -.5 * invp[i];
+  }
+  CK(cudaMemcpy((void*)b.spline_invp, invp, sizeof(invp), cudaMemcpyHostToDevice), "upload spline");
+  CK(cudaMemcpy((void*)b.spline_p, p, sizeof(p), cudaMemcpyHostToDevice), "upload spline");
+  if ((rc = make_twiddles(c, s.nfft, -1, &c->tw_fwd))) return rc;
+  if ((rc = make_twiddles(c, s.Ninterp, +1, &c->tw_inv))) return rc;
+  if ((rc = make_twiddles(c, s.nfftf, -1, &c->tw_main))) return rc;
+  for (int k = 0; k < 4; k++) {
+    b.tw_fwd[k] = c->tw_fwd.p[k];
+    b.tw_inv[k] = c->tw_inv.p[k];
+    b.tw_main[k] = c->tw_main.p[k];
+  }
+  if ((rc = upload_data(c, det))) return rc;
+  c->eng = c->fp64 ? pa::make_engine_f64(b) : pa::make_engine_f32(b, c->cfg.phase_mode);
+  if (!c->eng) return fail(c, PA_ERR_NOMEM, "engine allocation failed");
+  return PA_OK;
+}
+
+extern "C" {
+
+const char* pa_version(void) { return "polgraw-gb300 1.0 (sm_103a)"; }
+
+int pa_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+const char* pa_last_error(const pa_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+pa_ctx* pa_create(const pa_settings* sett, const pa_detector* det, int nifo, const pa_config* cfg,
+                  int* status) {
+  char why[256];
+  int st = PA_OK;
+  if (!sett || !det) {
+    fail(nullptr, PA_ERR_ARG, "null settings or detectors");
+    if (status) *status = PA_ERR_ARG;
+    return nullptr;
+  }
+  if (validate(sett, nifo, cfg, why, sizeof why)) {
+    fail(nullptr, PA_ERR_ARG, "%s", why);
+    if (status) *status = PA_ERR_ARG;
+    return nullptr;
+  }
+  for (int n = 0; n < nifo; n++)
+    if (!det[n].xDat || !det[n].DetSSB || !(det[n].sig2 > 0)) {
+      fail(nullptr, PA_ERR_ARG, "detector %d: missing data or sig2 <= 0", n);
+      if (status) *status = PA_ERR_ARG;
+      return nullptr;
+    }
+  int ndev = pa_device_count();
+  const int dev = cfg ? cfg->device : 0;
+  if (ndev <= 0 || dev < 0 || dev >= ndev) {
+    fail(nullptr, PA_ERR_NODEV, "no CUDA device %d (found %d)", dev, ndev);
+    if (status) *status = PA_ERR_NODEV;
+    return nullptr;
+  }
+  pa_ctx* c = new pa_ctx();
+  c->sett = *sett;
+  c->nifo = nifo;
+  if (cfg) c->cfg = *cfg;
+  else memset(&c->cfg, 0, sizeof(c->cfg));
+  c->fp64 = c->cfg.precision == PA_PREC_FP64;
+  c->rsz = c->fp64 ? 8 : 4;
+  c->dev = dev;
+  if (sett->numlines_band > 0) c->lines.assign(sett->lines, sett->lines + 2 * sett->numlines_band);
+  c->sett.lines = c->lines.empty() ? nullptr : c->lines.data();
+  st = build_ctx(c, det);
+  if (st != PA_OK) {
+    g_create_error = c->err;
+    pa_destroy(c);
+    if (status) *status = st;
+    return nullptr;
+  }
+  if (status) *status = PA_OK;
+  return c;
+}
+
+int pa_set_data(pa_ctx* c, const pa_detector* det, int nifo) {
+  if (!c || !det || nifo != c->nifo) return fail(c, PA_ERR_ARG, "pa_set_data: bad arguments");
+  CK(cudaSetDevice(c->dev), "cudaSetDevice");
+  for (int n = 0; n < nifo; n++)
+    if (!det[n].xDat || !det[n].DetSSB || !(det[n].sig2 > 0))
+      return fail(c, PA_ERR_ARG, "detector %d: missing data or sig2 <= 0", n);
+  return upload_data(c, det);
+}
+
+void pa_destroy(pa_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->dev);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  delete c->eng;
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->h_cand) cudaFreeHost(c->h_cand);
+  if (c->h_ncand) cudaFreeHost(c->h_ncand);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+long long pa_kernel_launches(const pa_ctx* c) {
+  if (!c) return 0;
+  return (c->eng ? c->eng->launches() : 0) + c->extra_launches;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------
+// job_core host logic
+
+namespace {
+
+struct SkyHost {
+  int pm, mm, nn;
+  int inside;
+  double sgnlt2, sgnlt3, het0;
+  int smin, smax, nss;
+  pa::SkyArgs args;
+};
+
+// auxi.c:16-24
+void lin2ast(double be1, double be2, int pm, double sepsm, double cepsm, double* sinal, double* cosal,
+             double* sindel, double* cosdel) {
+  *sindel = be1 * sepsm - (2 * pm - 3) * sqrt(1. - SQR(be1) - SQR(be2)) * cepsm;
+  *cosdel = sqrt(1. - SQR(*sindel));
+  *sinal = (be1 - sepsm * (*sindel)) / (cepsm * (*cosdel));
+  *cosal = be2 / (*cosdel);
+}
+
+void sky_setup(const pa_ctx* c, int pm, int mm, int nn, const pa_opts* o, int sst, int spndr1,
+               SkyHost* h) {
+  const pa_settings& s = c->sett;
+  const double* M = s.M;
+  memset(h, 0, sizeof(*h));
+  h->pm = pm;
+  h->mm = mm;
+  h->nn = nn;
+  double al1 = nn * M[10] + mm * M[14];
+  double al2 = nn * M[11] + mm * M[15];
+  if ((SQR(al1) + SQR(al2)) / SQR(s.oms) > 1.) {  // jobcore.c:248
+    h->inside = 0;
+    return;
+  }
+  h->inside = 1;
+  double sinalt, cosalt, sindelt, cosdelt;
+  lin2ast(al1 / s.oms, al2 / s.oms, pm, s.sepsm, s.cepsm, &sinalt, &cosalt, &sindelt, &cosdelt);
+  h->sgnlt2 = asin(sindelt);
+  h->sgnlt3 = fmod(atan2(sinalt, cosalt) + 2. * M_PI, 2. * M_PI);
+  h->het0 = fmod(nn * M[8] + mm * M[12], M[0]);
+  // jobcore.c:424-444
+  int smin = sst, smax = spndr1;
+  if (!o->use_range) {
+    smin = trunc((s.Smin - nn * M[9] - mm * M[13]) / M[5]);
+    smax = trunc(-(nn * M[9] + mm * M[13] + s.Smax) / M[5]);
+    if (smin > smax) std::swap(smin, smax);
+  }
+  if (o->s0_flag) smin = smax;
+  h->smin = smin;
+  h->smax = smax;
+  h->nss = smax >= smin ? smax - smin + 1 : 0;
+  pa::SkyArgs& a = h->args;
+  a.het0 = h->het0;
+  a.oms = s.oms;
+  a.sinal = sinalt;
+  a.cosal = cosalt;
+  a.sindel = sindelt;
+  a.cosdel = cosdelt;
+  a.nS[0] = cosalt * cosdelt;
+  a.nS[1] = sinalt * cosdelt;
+  a.nS[2] = sindelt;
+  for (int n = 0; n < c->nifo; n++) {
+    a.shft1[n] = a.nS[0] * c->det0[n][0] + a.nS[1] * c->det0[n][1] + a.nS[2] * c->det0[n][2];
+    a.cosalfr[n] = cosalt * c->dc[n].cphir + sinalt * c->dc[n].sphir;
+    a.sinalfr[n] = sinalt * c->dc[n].cphir - cosalt * c->dc[n].sphir;
+  }
+  a.s1_0 = o->s0_flag ? 0. : nn * M[9] + mm * M[13];
+  a.M5 = o->s0_flag ? 0. : M[5];
+  a.M0 = M[0];
+  a.M4 = M[4];
+  a.task = 0;
+}
+
+int enqueue_sky(pa_ctx* c, const SkyHost& h, const pa_opts* o, int task, void* Fdbg, int Fss) {
+  pa::SkyArgs a = h.args;
+  a.task = task;
+  cudaError_t e = c->eng->prelude(a, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "prelude launch");
+  if (Fdbg) {
+    e = c->eng->spindowns(a, Fss, 1, o->trl, o->white_flag, o->s0_flag, c->stream, Fdbg);
+    if (e != cudaSuccess) return cuda_fail(c, e, "spindown launch");
+    return PA_OK;
+  }
+  for (int ss = h.smin; ss <= h.smax; ss += c->b.sbatch) {
+    const int nb = std::min(c->b.sbatch, h.smax - ss + 1);
+    e = c->eng->spindowns(a, ss, nb, o->trl, o->white_flag, o->s0_flag, c->stream, nullptr);
+    if (e != cudaSuccess) return cuda_fail(c, e, "spindown launch");
+  }
+  return PA_OK;
+}
+
+bool cand_less(const pa::DevCand& x, const pa::DevCand& y) {
+  if (x.task != y.task) return x.task < y.task;
+  if (x.ss != y.ss) return x.ss < y.ss;
+  return x.ii < y.ii;
+}
+
+// Runs the sky points, gathers the device candidates (sorted to the serial
+// order) into `out`.  Grows the device candidate buffer and re-runs when it
+// overflowed.
+int run_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o, std::vector<pa::DevCand>* out) {
+  CK(cudaSetDevice(c->dev), "cudaSetDevice");
+  for (int attempt = 0; attempt < 3; attempt++) {
+    CK(cudaMemsetAsync(c->b.ncand, 0, sizeof(int), c->stream), "memset");
+    for (size_t t = 0; t < hs.size(); t++) {
+      if (!hs[t].inside || hs[t].nss == 0) continue;
+      int rc = enqueue_sky(c, hs[t], o, (int)t, nullptr, 0);
+      if (rc) return rc;
+    }
+    CK(cudaMemcpyAsync(c->h_ncand, c->b.ncand, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "copy count");
+    CK(cudaStreamSynchronize(c->stream), "search");
+    const int n = *c->h_ncand;
+    if (n <= c->b.cand_cap) {
+      if (n > 0) {
+        CK(cudaMemcpyAsync(c->h_cand, c->b.cand, sizeof(pa::DevCand) * (size_t)n, cudaMemcpyDeviceToHost,
+                           c->stream), "copy candidates");
+        CK(cudaStreamSynchronize(c->stream), "copy candidates");
+      }
+      out->assign(c->h_cand, c->h_cand + n);
+      std::sort(out->begin(), out->end(), cand_less);
+      return PA_OK;
+    }
+    // grow and retry
+    const int ncap = n + n / 2;
+    void* p = nullptr;
+    CK(cudaMalloc(&p, sizeof(pa::DevCand) * (size_t)ncap), "cudaMalloc");
+    c->allocs.push_back(p);
+    c->b.cand = (pa::DevCand*)p;
+    cudaFreeHost(c->h_cand);
+    c->h_cand = nullptr;
+    CK(cudaMallocHost((void**)&c->h_cand, sizeof(pa::DevCand) * (size_t)ncap), "cudaMallocHost");
+    c->b.cand_cap = ncap;
+    delete c->eng;
+    c->eng = c->fp64 ? pa::make_engine_f64(c->b) : pa::make_engine_f32(c->b, c->cfg.phase_mode);
+  }
+  return fail(c, PA_ERR_CAPACITY, "device candidate buffer overflow");
+}
+
+// jobcore.c:670-687 record for one candidate; returns 0 when vetoed
+int make_record(const pa_ctx* c, const SkyHost& h, const pa_opts* o, const pa::DevCand& d, double rec[5]) {
+  const pa_settings& s = c->sett;
+  const double* M = s.M;
+  const int ss = d.ss, nn = h.nn, mm = h.mm;
+  double het1 = fmod(ss * M[4], M[0]);
+  if (het1 < 0) het1 += M[0];
+  const double sgnl0 = h.het0 + het1;
+  rec[0] = 2. * M_PI * d.ii / ((double)s.fftpad * s.nfft) + sgnl0;
+  rec[1] = o->s0_flag ? 0. : ss * M[5] + nn * M[9] + mm * M[13];
+  rec[2] = h.sgnlt2;
+  rec[3] = h.sgnlt3;
+  rec[4] = sqrt(2. * (d.F - s.nd));
+  for (int k = 0; k < s.numlines_band; k++)
+    if (rec[0] >= s.lines[2 * k] && rec[0] <= s.lines[2 * k + 1]) return 0;
+  return 1;
+}
+
+int append_records(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o,
+                   const std::vector<pa::DevCand>& cands, int* sgnlc, double* sgnlv, int cap,
+                   pa_cand_idx* idx, int* FNum, int* needed) {
+  std::vector<double> recs;
+  std::vector<pa_cand_idx> ids;
+  recs.reserve(cands.size() * PA_NPAR);
+  for (const pa::DevCand& d : cands) {
+    const SkyHost& h = hs[d.task];
+    double rec[5];
+    if (!make_record(c, h, o, d, rec)) continue;
+    recs.insert(recs.end(), rec, rec + 5);
+    pa_cand_idx x;
+    x.pm = h.pm;
+    x.mm = h.mm;
+    x.nn = h.nn;
+    x.ss = d.ss;
+    x.ii = d.ii;
+    x.F = (float)d.F;
+    ids.push_back(x);
+  }
+  const int total = (int)ids.size();
+  if (needed) *needed = *sgnlc + total;
+  if (*sgnlc + total > cap) return fail(c, PA_ERR_CAPACITY, "candidate buffer too small: need %d", *sgnlc + total);
+  memcpy(sgnlv + (size_t)PA_NPAR * (*sgnlc), recs.data(), sizeof(double) * recs.size());
+  if (idx) memcpy(idx + *sgnlc, ids.data(), sizeof(pa_cand_idx) * ids.size());
+  *sgnlc += total;
+  int nss = 0;
+  for (const SkyHost& h : hs)
+    if (h.inside) nss += h.nss;
+  *FNum += nss;
+  return PA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pa_job_core(pa_ctx* c, int pm, int mm, int nn, const pa_opts* o, const pa_range* r, int* sgnlc,
+                double* sgnlv, int cap, pa_cand_idx* idx, int* FNum, int* needed) {
+  if (!c || !o || !r || !sgnlc || !sgnlv || !FNum || cap < 0) return fail(c, PA_ERR_ARG, "pa_job_core: bad arguments");
+  pa_sky t{pm, mm, nn};
+  return pa_search_batch(c, &t, 1, o, r, sgnlc, sgnlv, cap, idx, FNum, needed);
+}
+
+int pa_search_batch(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o, const pa_range* r,
+                    int* sgnlc, double* sgnlv, int cap, pa_cand_idx* idx, int* FNum, int* needed) {
+  if (!c || !tasks || ntasks < 0 || !o || !r || !sgnlc || !sgnlv || !FNum || cap < 0)
+    return fail(c, PA_ERR_ARG, "pa_search_batch: bad arguments");
+  if (needed) *needed = *sgnlc;
+  std::vector<SkyHost> hs(ntasks);
+  for (int t = 0; t < ntasks; t++) {
+    // the sky loop resets sst to spndr[0] after each sky point (jobcore.c:123)
+    const int sst = t == 0 ? r->sst : r->spndr[0];
+    sky_setup(c, tasks[t].pm, tasks[t].mm, tasks[t].nn, o, sst, r->spndr[1], &hs[t]);
+  }
+  std::vector<pa::DevCand> cands;
+  int rc = run_tasks(c, hs, o, &cands);
+  if (rc) return rc;
+  return append_records(c, hs, o, cands, sgnlc, sgnlv, cap, idx, FNum, needed);
+}
+
+int pa_debug_prelude(pa_ctx* c, int pm, int mm, int nn, double* xa, double* xb, double* aa, double* bb) {
+  if (!c) return PA_ERR_ARG;
+  CK(cudaSetDevice(c->dev), "cudaSetDevice");
+  pa_opts o;
+  memset(&o, 0, sizeof(o));
+  o.use_range = 1;
+  SkyHost h;
+  sky_setup(c, pm, mm, nn, &o, 0, 0, &h);
+  if (!h.inside) return fail(c, PA_ERR_ARG, "sky point outside the grid disk");
+  cudaError_t e = c->eng->prelude(h.args, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "prelude");
+  const size_t n = (size_t)c->nifo * 2 * c->sett.N;
+  std::vector<char> buf(n * 2 * c->rsz);
+  double sums[4];
+  CK(cudaMemcpyAsync(buf.data(), c->b.xm, buf.size(), cudaMemcpyDeviceToHost, c->stream), "copy");
+  CK(cudaMemcpyAsync(sums, c->b.sums, sizeof(sums), cudaMemcpyDeviceToHost, c->stream), "copy");
+  CK(cudaStreamSynchronize(c->stream), "prelude");
+  const int N = c->sett.N;
+  for (int d = 0; d < c->nifo; d++)
+    for (int arr = 0; arr < 2; arr++) {
+      double* dst = arr == 0 ? xa : xb;
+      if (!dst) continue;
+      for (int i = 0; i < N; i++) {
+        const size_t src = ((size_t)d * 2 + arr) * N + i;
+        double re, im;
+        if (c->fp64) {
+          re = ((double*)buf.data())[2 * src];
+          im = ((double*)buf.data())[2 * src + 1];
+        } else {
+          re = ((float*)buf.data())[2 * src];
+          im = ((float*)buf.data())[2 * src + 1];
+        }
+        dst[2 * ((size_t)d * N + i)] = re;
+        dst[2 * ((size_t)d * N + i) + 1] = im;
+      }
+    }
+  if (aa) *aa = sums[0];
+  if (bb) *bb = sums[1];
+  return PA_OK;
+}
+
+int pa_debug_fstat(pa_ctx* c, int pm, int mm, int nn, int ss, const pa_opts* o, double* F) {
+  if (!c || !o || !F) return PA_ERR_ARG;
+  CK(cudaSetDevice(c->dev), "cudaSetDevice");
+  SkyHost h;
+  sky_setup(c, pm, mm, nn, o, ss, ss, &h);
+  if (!h.inside) return fail(c, PA_ERR_ARG, "sky point outside the grid disk");
+  const int bins = c->b.bins;
+  void* dF = nullptr;
+  CK(cudaMalloc(&dF, c->rsz * (size_t)bins), "cudaMalloc");
+  CK(cudaMemsetAsync(c->b.ncand, 0, sizeof(int), c->stream), "memset");
+  int rc = enqueue_sky(c, h, o, 0, dF, ss);
+  std::vector<char> buf(c->rsz * (size_t)bins);
+  if (!rc) {
+    cudaError_t e = cudaMemcpyAsync(buf.data(), dF, buf.size(), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(c, e, "debug fstat");
+  }
+  cudaFree(dF);
+  if (rc) return rc;
+  for (int i = 0; i < bins; i++) F[i] = c->fp64 ? ((double*)buf.data())[i] : ((float*)buf.data())[i];
+  return PA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,665 @@
+// pa_engine.cuh -- device kernels of the coherent-search hot path and the
+// templated engine that enqueues them.  Included by the per-precision
+// translation units only.
+//
+// Reference correspondence (search/network/src-cpu):
+//   k_prelude_mod   modvir (settings.c:281-325), shft/shftf/_tmp1 and the
+//                   prelude phase modulation (jobcore.c:277-313)
+//   resample FFTs   jobcore.c:319-362 (pass A/B with PlainLoader, RemapLoader)
+//   k_spline_fwd/bwd spline() (auxi.c:56-81), FP64 chunked recurrences
+//   k_splint        splint/splintpad (auxi.c:83-122) + 1/sig2 (jobcore.c:386-389)
+//   k_prelude_sums  aa, bb (jobcore.c:375-393)
+//   SpinLoader      spindown phase modulation (jobcore.c:455-623)
+//   FstatStore      F = |Xa|^2/aa + |Xb|^2/bb (jobcore.c:635-638)
+//   k_blockmean     FStat() block means (auxi.c:214-240)
+//   k_threshold     threshold, run clustering, argmax (jobcore.c:659-669)
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#include "pa_engine.h"
+#include "pa_fft.cuh"
+
+namespace pa {
+
+enum { PM_F64 = 0, PM_FIXED = 1, PM_FF = 2 };
+
+constexpr double kTwoPiHi = 6.283185307179586232;       // 2 pi rounded to double
+constexpr double kTwoPiLo = 2.4492935982947064e-16;      // 2 pi - kTwoPiHi
+constexpr double kInvTwoPi = 0.15915494309189535;
+constexpr double kTurnsPerRad64 = 2.9358905032820014e18;  // 2^64 / (2 pi)
+// 2 pi as the sum of three floats with 12, 24 and 24 significant bits; k*A
+// is exact for |k| < 2^12
+constexpr float kTwoPiF_A = 6.28125f;
+constexpr float kTwoPiF_B = 1.9353071693331003e-3f;
+constexpr float kTwoPiF_C = 1.0253131677018246e-11f;
+constexpr float kInvTwoPiF = 0.15915494309189533577f;
+
+// ------------------------------------------------------------------
+// prelude: modvir + time shift + prelude phase modulation
+
+template <typename R, int PM>
+__global__ void __launch_bounds__(256)
+    k_prelude_mod(const double* __restrict__ xDat, const double* __restrict__ DetSSB,
+                  const R* __restrict__ cosmodf, const R* __restrict__ sinmodf,
+                  const DetConst* __restrict__ dc, const SkyArgs sky, int N,
+                  typename CT<R>::T* __restrict__ xin, double* __restrict__ shftf, void* ph0,
+                  void* ph1, double* __restrict__ part) {
+  typedef typename CT<R>::T T;
+  const int d = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double a2 = 0., b2 = 0.;
+  if (i < N) {
+    const DetConst& k = dc[d];
+    // modvir, settings.c:303-322
+    const R cosalfr = (R)sky.cosalfr[d], sinalfr = (R)sky.sinalfr[d];
+    const R cm = cosmodf[i], sm = sinmodf[i];
+    const R c = cosalfr * cm + sinalfr * sm;
+    const R s = sinalfr * cm - cosalfr * sm;
+    const R cosdel = (R)sky.cosdel, sindel = (R)sky.sindel;
+    const R c2d = cosdel * cosdel, c2sd = sindel * cosdel;
+    const R c2s = (R)2 * c * c, cs = c * s;
+    const R k0 = (R)k.amod[0], k1 = (R)k.amod[1], k2 = (R)k.amod[2], k3 = (R)k.amod[3],
+            k4 = (R)k.amod[4], k5 = (R)k.amod[5], k6 = (R)k.amod[6], k7 = (R)k.amod[7],
+            k8 = (R)k.amod[8];
+    const R two_m = (R)2 - c2d;
+    const R aa = k0 * two_m * c2s + k1 * two_m * (R)2 * cs + k2 * c2sd * c + k3 * c2sd * s -
+                 k0 * two_m + k4 * c2d;
+    const R bb = k5 * sindel * c2s + k6 * sindel * (R)2 * cs + k7 * cosdel * c + k8 * cosdel * s -
+                 k5 * sindel;
+    a2 = (double)aa * (double)aa;
+    b2 = (double)bb * (double)bb;
+    // shft, shftf, _tmp1 (jobcore.c:285-295), FP64
+    const double* D = DetSSB + 3 * ((size_t)d * N + i);
+    const double shft = sky.nS[0] * D[0] + sky.nS[1] * D[1] + sky.nS[2] * D[2];
+    shftf[(size_t)d * N + i] = shft - sky.shft1[d];
+    const double di = (double)i;
+    const double tmp1 = di * di + (double)(2 * i) * shft;
+    const size_t o = (size_t)d * N + i;
+    if (PM == PM_FIXED) {
+      // spindown phase s1(ss) tmp1 = s1_0 tmp1 + ss (M5 tmp1); both terms as
+      // 64-bit fixed-point fractions of a turn
+      double fa = sky.s1_0 * tmp1 * kInvTwoPi;
+      fa -= floor(fa);
+      double fb = sky.M5 * tmp1 * kInvTwoPi;
+      fb -= floor(fb);
+      reinterpret_cast<uint64_t*>(ph0)[o] = (uint64_t)__double2ull_rn(fa * 18446744073709551616.0);
+      reinterpret_cast<uint64_t*>(ph1)[o] = (uint64_t)__double2ull_rn(fb * 18446744073709551616.0);
+    } else if (PM == PM_FF) {
+      const float hi = (float)tmp1;
+      reinterpret_cast<float2*>(ph0)[o] = make_float2(hi, (float)(tmp1 - (double)hi));
+    } else {
+      reinterpret_cast<double*>(ph0)[o] = tmp1;
+    }
+    // prelude phase het0 i + oms shft (jobcore.c:299), FP64
+    const double phase = sky.het0 * di + sky.oms * shft;
+    R sp, cp;
+    if (sizeof(R) == 8) {
+      double sd, cd;
+      sincos(phase, &sd, &cd);
+      sp = (R)sd;
+      cp = (R)cd;
+    } else {
+      const double kk = rint(phase * kInvTwoPi);
+      double r = fma(-kk, kTwoPiHi, phase);
+      r = fma(-kk, kTwoPiLo, r);
+      float sf, cf;
+      sincosf((float)r, &sf, &cf);
+      sp = (R)sf;
+      cp = (R)cf;
+    }
+    const R x = (R)xDat[(size_t)d * N + i];
+    const R xa = x * aa, xb = x * bb;
+    // x a exp(-i phase)
+    xin[((size_t)d * 2 + 0) * N + i] = mk(xa * cp, -xa * sp);
+    xin[((size_t)d * 2 + 1) * N + i] = mk(xb * cp, -xb * sp);
+  }
+  // deterministic block reduction of a^2, b^2
+  __shared__ double red[2][8];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    a2 += __shfl_xor_sync(0xffffffffu, a2, off);
+    b2 += __shfl_xor_sync(0xffffffffu, b2, off);
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][w] = a2;
+    red[1][w] = b2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sa = 0., sb = 0.;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      sa += red[0][k];
+      sb += red[1][k];
+    }
+    part[((size_t)d * gridDim.x + blockIdx.x) * 2 + 0] = sa;
+    part[((size_t)d * gridDim.x + blockIdx.x) * 2 + 1] = sb;
+  }
+}
+
+// aa = sum_n (sum_i a^2)/sig2_n, bb likewise (jobcore.c:375-393)
+static __global__ void k_prelude_sums(const double* __restrict__ part, int nblocks, int nifo,
+                               const DetConst* __restrict__ dc, double* __restrict__ sums) {
+  __shared__ double red[2][32];
+  double aa = 0., bb = 0.;
+  for (int d = 0; d < nifo; ++d) {
+    double sa = 0., sb = 0.;
+    for (int b = threadIdx.x; b < nblocks; b += 32) {
+      sa += part[((size_t)d * nblocks + b) * 2 + 0];
+      sb += part[((size_t)d * nblocks + b) * 2 + 1];
+    }
+    red[0][threadIdx.x] = sa;
+    red[1][threadIdx.x] = sb;
+    __syncwarp();
+    if (threadIdx.x == 0) {
+      double ta = 0., tb = 0.;
+      for (int k = 0; k < 32; ++k) {
+        ta += red[0][k];
+        tb += red[1][k];
+      }
+      aa += ta / dc[d].sig2;
+      bb += tb / dc[d].sig2;
+    }
+    __syncwarp();
+  }
+  if (threadIdx.x == 0) {
+    sums[0] = aa;
+    sums[1] = bb;
+    sums[2] = 1.0 / aa;
+    sums[3] = 1.0 / bb;
+  }
+}
+
+// ------------------------------------------------------------------
+// FFT loaders / storers
+
+template <typename R> struct PlainLoader {
+  typedef typename CT<R>::T T;
+  const T* in;   // [batch][2][ld]
+  int len, ld;
+  __device__ __forceinline__ void prologue(int, char*) const {}
+  __device__ __forceinline__ void load2(int batch, int n, T& a, T& b, const char*) const {
+    if (n < len) {
+      a = in[((size_t)batch * 2 + 0) * ld + n];
+      b = in[((size_t)batch * 2 + 1) * ld + n];
+    } else {
+      a = b = mk((R)0, (R)0);
+    }
+  }
+};
+
+// Spectrum remap of jobcore.c:338-352: bins [0, nyqst) stay, [nyqst, nfft)
+// move up by Ninterp - nfft, the gap is zero.
+template <typename R> struct RemapLoader {
+  typedef typename CT<R>::T T;
+  const T* spec;   // [batch][2][nfft]
+  int nfft, nyqst, shift;
+  __device__ __forceinline__ void prologue(int, char*) const {}
+  __device__ __forceinline__ void load2(int batch, int j, T& a, T& b, const char*) const {
+    int idx = j < nyqst ? j : (j < nyqst + shift ? -1 : j - shift);
+    if (idx >= 0) {
+      a = spec[((size_t)batch * 2 + 0) * nfft + idx];
+      b = spec[((size_t)batch * 2 + 1) * nfft + idx];
+    } else {
+      a = b = mk((R)0, (R)0);
+    }
+  }
+};
+
+struct SpinCta {
+  double het1, s1;
+  uint64_t H;
+  long long ss;
+  float s1h, s1l, h1h, h1l;
+};
+
+// Phase-modulated detector sum of the spindown loop (jobcore.c:455-623):
+//   x_{a,b}[n] = sum_d xm_{a,b,d}[n] exp(-i (het1 n + s1 tmp1_d[n]))  (n < N)
+template <typename R, int PM> struct SpinLoader {
+  typedef typename CT<R>::T T;
+  const T* xm;       // [nifo][2][N]
+  const void* ph0;
+  const void* ph1;
+  int N, nifo, ss0, s0_flag;
+  double M0, M4, M5, s1_0;
+
+  __device__ __forceinline__ void prologue(int batch, char* sm) const {
+    if (threadIdx.x == 0) {
+      SpinCta* p = reinterpret_cast<SpinCta*>(sm);
+      const int ss = ss0 + batch;
+      double het1 = fmod(ss * M4, M0);
+      if (het1 < 0) het1 += M0;
+      const double s1 = s0_flag ? 0. : ss * M5 + s1_0;
+      p->het1 = het1;
+      p->s1 = s1;
+      p->H = (uint64_t)__double2ull_rn(het1 * kTurnsPerRad64);
+      p->ss = s0_flag ? 0 : ss;
+      p->s1h = (float)s1;
+      p->s1l = (float)(s1 - (double)p->s1h);
+      p->h1h = (float)het1;
+      p->h1l = (float)(het1 - (double)p->h1h);
+    }
+  }
+
+  __device__ __forceinline__ void load2(int, int n, T& va, T& vb, const char* sm) const {
+    va = vb = mk((R)0, (R)0);
+    if (n >= N) return;
+    const SpinCta* p = reinterpret_cast<const SpinCta*>(sm);
+    R accx = 0, accy = 0, bccx = 0, bccy = 0;
+    double base = 0.;
+    uint64_t ibase = 0;
+    if (PM == PM_FIXED) ibase = p->H * (uint64_t)n;
+    else if (PM == PM_F64) base = p->het1 * (double)n;
+    for (int d = 0; d < nifo; ++d) {
+      const size_t o = (size_t)d * N + n;
+      R sn, cs;
+      if (sizeof(R) == 8) {
+        const double t1 = reinterpret_cast<const double*>(ph0)[o];
+        const double ph = p->het1 * (double)n + p->s1 * t1;
+        double sd, cd;
+        sincos(ph, &sd, &cd);
+        sn = (R)sd;
+        cs = (R)cd;
+      } else if (PM == PM_F64) {
+        const double t1 = reinterpret_cast<const double*>(ph0)[o];
+        const double ph = fma(p->s1, t1, base);
+        const double kk = rint(ph * kInvTwoPi);
+        double r = fma(-kk, kTwoPiHi, ph);
+        r = fma(-kk, kTwoPiLo, r);
+        float sf, cf;
+        sincosf((float)r, &sf, &cf);
+        sn = (R)sf;
+        cs = (R)cf;
+      } else if (PM == PM_FIXED) {
+        const uint64_t A = reinterpret_cast<const uint64_t*>(ph0)[o];
+        const uint64_t B = reinterpret_cast<const uint64_t*>(ph1)[o];
+        const uint64_t t = A + (uint64_t)p->ss * B + ibase;
+        // fraction of a turn as a signed value in [-1/2, 1/2) -> pi * x
+        const float x = (float)(long long)t * 1.0842021724855044e-19f;  // 2^-63
+        float sf, cf;
+        sincospif(x, &sf, &cf);
+        sn = (R)sf;
+        cs = (R)cf;
+      } else {
+        // compensated float-float phase
+        const float2 tt = reinterpret_cast<const float2*>(ph0)[o];
+        float p1 = p->s1h * tt.x;
+        float e1 = fmaf(p->s1h, tt.x, -p1);
+        e1 = fmaf(p->s1h, tt.y, e1);
+        e1 = fmaf(p->s1l, tt.x, e1);
+        const float nf = (float)n;
+        float p2 = p->h1h * nf;
+        float e2 = fmaf(p->h1h, nf, -p2);
+        e2 = fmaf(p->h1l, nf, e2);
+        const float s = p1 + p2;
+        const float bb = s - p1;
+        const float err = (p1 - (s - bb)) + (p2 - bb);
+        const float e = err + e1 + e2;
+        const float kk = rintf(s * kInvTwoPiF);
+        float r = fmaf(-kk, kTwoPiF_A, s);
+        r = fmaf(-kk, kTwoPiF_B, r);
+        r = fmaf(-kk, kTwoPiF_C, r);
+        r += e;
+        float sf, cf;
+        sincosf(r, &sf, &cf);
+        sn = (R)sf;
+        cs = (R)cf;
+      }
+      const T xa = xm[((size_t)d * 2 + 0) * N + n];
+      const T xb = xm[((size_t)d * 2 + 1) * N + n];
+      // x * (cos - i sin)
+      accx += xa.x * cs + xa.y * sn;
+      accy += xa.y * cs - xa.x * sn;
+      bccx += xb.x * cs + xb.y * sn;
+      bccy += xb.y * cs - xb.x * sn;
+    }
+    va = mk(accx, accy);
+    vb = mk(bccx, bccy);
+  }
+};
+
+// Complex output with a scale factor (resampling FFTs).
+template <typename R> struct CStore {
+  typedef typename CT<R>::T T;
+  T* out;   // [batch][2][ldo]
+  int ldo;
+  R scale;
+  __device__ __forceinline__ void store(int batch, int t, const T* s, const Geom& g) const {
+    constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
+    const int rmask = g.Rr - 1;
+    for (int w = threadIdx.x; w < E; w += NT) {
+      const int r = w & rmask, rest = w >> g.logRr;
+      const int arr = rest & 1, k2 = rest >> 1;
+      const int k = (t << g.logRr) + r + (k2 << g.logL1);
+      const T v = s[(k2 << (g.logRr + 1)) + arr * g.Rr + r];
+      out[((size_t)batch * 2 + arr) * ldo + k] = mk(v.x * scale, v.y * scale);
+    }
+  }
+};
+
+// F-statistic epilogue: F[k] = |Xa[k]|^2 / aa + |Xb[k]|^2 / bb, k in [nmin, nmax)
+template <typename R> struct FstatStore {
+  typedef typename CT<R>::T T;
+  R* F;             // [batch][bins]
+  const double* sums;
+  int nmin, nmax, bins;
+  __device__ __forceinline__ void store(int batch, int t, const T* s, const Geom& g) const {
+    constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
+    const R ia = (R)sums[2], ib = (R)sums[3];
+    const int rmask = g.Rr - 1;
+    R* Fb = F + (size_t)batch * bins - nmin;
+    for (int w = threadIdx.x; w < (E >> 1); w += NT) {
+      const int r = w & rmask, k2 = w >> g.logRr;
+      const int k = (t << g.logRr) + r + (k2 << g.logL1);
+      if (k >= nmin && k < nmax) {
+        const T xa = s[(k2 << (g.logRr + 1)) + r];
+        const T xb = s[(k2 << (g.logRr + 1)) + g.Rr + r];
+        Fb[k] = (xa.x * xa.x + xa.y * xa.y) * ia + (xb.x * xb.x + xb.y * xb.y) * ib;
+      }
+    }
+  }
+};
+
+// ------------------------------------------------------------------
+// spline (auxi.c:56-81): chunked FP64 recurrences.  The forward sweep
+// u_i = (-u_{i-1}/2 + 3 d_i) invp_i has |dU_i/dU_{i-1}| -> 2 - sqrt(3) = 0.268
+// and the back substitution y2_k = p_k y2_{k+1} + u_k likewise, so a chunk
+// can start kWarm steps early from zero: the start error shrinks by
+// 0.268^kWarm < 1e-18.  Chunks whose warm start reaches the array ends start
+// from the exact boundary values u_0 = 0, y2_{n-1} = 0.
+constexpr int kSplineChunk = 64;
+constexpr int kSplineWarm = 32;
+
+template <typename R>
+__global__ void __launch_bounds__(128)
+    k_spline_fwd(const typename CT<R>::T* __restrict__ y, int ldy, double2* __restrict__ u, int n,
+                 int nchunks, int narr, const double* __restrict__ invp) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= nchunks * narr) return;
+  const int q = gid / nchunks, c = gid - q * nchunks;
+  const typename CT<R>::T* yq = y + (size_t)q * ldy;
+  double2* uq = u + (size_t)q * n;
+  const int lo = c * kSplineChunk;
+  const int hi = min(lo + kSplineChunk, n - 1);
+  if (c == 0) uq[0] = make_double2(0., 0.);
+  int i = max(1, lo - kSplineWarm);
+  double ux = 0., uy = 0.;
+  double pxr = (double)yq[i - 1].x, pyr = (double)yq[i - 1].y;
+  double cxr = (double)yq[i].x, cyr = (double)yq[i].y;
+  for (; i < hi; ++i) {
+    const double nxr = (double)yq[i + 1].x, nyr = (double)yq[i + 1].y;
+    const double dx = pxr - 2. * cxr + nxr, dy = pyr - 2. * cyr + nyr;
+    const double ip = invp[i < 64 ? i : 63];
+    ux = (-.5 * ux + 3. * dx) * ip;
+    uy = (-.5 * uy + 3. * dy) * ip;
+    if (i >= lo) uq[i] = make_double2(ux, uy);
+    pxr = cxr;
+    pyr = cyr;
+    cxr = nxr;
+    cyr = nyr;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128)
+    k_spline_bwd(const double2* __restrict__ u, typename CT<R>::T* __restrict__ y2, int n,
+                 int nchunks, int narr, const double* __restrict__ ptab) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= nchunks * narr) return;
+  const int q = gid / nchunks, c = gid - q * nchunks;
+  const double2* uq = u + (size_t)q * n;
+  typename CT<R>::T* yq = y2 + (size_t)q * n;
+  const int lo = c * kSplineChunk;
+  const int hi = min(lo + kSplineChunk, n);
+  if (hi == n) yq[n - 1] = mk((R)0, (R)0);
+  const int kst = min(n - 2, hi - 1 + kSplineWarm);
+  double vx = 0., vy = 0.;
+  for (int k = kst; k >= lo; --k) {
+    const double p = ptab[k < 64 ? k : 63];
+    const double2 uk = uq[k];
+    vx = p * vx + uk.x;
+    vy = p * vy + uk.y;
+    if (k < hi) yq[k] = mk((R)vx, (R)vy);
+  }
+}
+
+// splint at x = interpftpad (i - shftf_i) (auxi.c:83-122), then / sig2
+template <typename R>
+__global__ void __launch_bounds__(256)
+    k_splint(const typename CT<R>::T* __restrict__ y, int ldy, const typename CT<R>::T* __restrict__ y2,
+             const double* __restrict__ shftf, const DetConst* __restrict__ dc, int N,
+             typename CT<R>::T* __restrict__ xm) {
+  typedef typename CT<R>::T T;
+  const int d = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int n = 2 * N;
+  const double x = 2 * (i - shftf[(size_t)d * N + i]);
+  const R is2 = (R)dc[d].inv_sig2;
+  for (int arr = 0; arr < 2; ++arr) {
+    const size_t q = (size_t)d * 2 + arr;
+    T v = mk((R)0, (R)0);
+    if (!(x < 0 || x > n - 1)) {
+      const int klo = (int)floor(x);
+      const int khi = klo + 1;
+      const int kh = khi < n ? khi : n - 1;
+      const R a = (R)(khi - x), b = (R)(x - klo);
+      const T ylo = y[q * ldy + klo], yhi = y[q * ldy + kh];
+      const T zlo = y2[q * n + klo], zhi = y2[q * n + kh];
+      const R ca = (a * a * a - a), cb = (b * b * b - b);
+      v.x = a * ylo.x + b * yhi.x + (ca * zlo.x + cb * zhi.x) / (R)6;
+      v.y = a * ylo.y + b * yhi.y + (ca * zlo.y + cb * zhi.y) / (R)6;
+    }
+    xm[q * N + i] = mk(v.x * is2, v.y * is2);
+  }
+}
+
+// ------------------------------------------------------------------
+// FStat normalisation and thresholding
+
+// mu_b = sum over the 4096-bin block b of F / (2*4096), auxi.c:228-232
+template <typename R>
+__global__ void __launch_bounds__(256)
+    k_blockmean(const R* __restrict__ F, int bins, int nblk, R* __restrict__ mu) {
+  const int b = blockIdx.x, sidx = blockIdx.y;
+  const R* f = F + (size_t)sidx * bins + (size_t)b * 4096;
+  R acc = 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) acc += f[k * 256 + threadIdx.x];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  __shared__ R red[8];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    R sum = 0;
+    for (int k = 0; k < 8; ++k) sum += red[k];
+    mu[(size_t)sidx * nblk + b] = sum / (R)(2 * 4096);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ R norm_f(const R* f, const R* m, int i, int nblk, int white) {
+  R v = f[i];
+  if (!white) {
+    const int b = i >> 12;
+    if (b < nblk) v = v / m[b];
+  }
+  return v;
+}
+
+// Runs of consecutive bins above trl produce one candidate at the run's
+// maximum, ties to the later bin (jobcore.c:659-669).
+template <typename R>
+__global__ void __launch_bounds__(256)
+    k_threshold(const R* __restrict__ F, int bins, int nblk, const R* __restrict__ mu, int white,
+                R trl, int nmin, int ss0, int task, DevCand* __restrict__ cand, int* __restrict__ ncand,
+                int cap, R* __restrict__ Fdbg) {
+  const int c = blockIdx.x, sidx = blockIdx.y;
+  const R* f = F + (size_t)sidx * bins;
+  const R* m = mu + (size_t)sidx * nblk;
+#pragma unroll 1
+  for (int k = 0; k < 16; ++k) {
+    const int i = c * 4096 + k * 256 + threadIdx.x;
+    if (i >= bins) break;
+    const R v = norm_f(f, m, i, nblk, white);
+    if (Fdbg) Fdbg[(size_t)sidx * bins + i] = v;
+    if (v > trl && (i == 0 || !(norm_f(f, m, i - 1, nblk, white) > trl))) {
+      int ii = i;
+      R Fc = v;
+      for (int j = i + 1; j < bins; ++j) {
+        const R w = norm_f(f, m, j, nblk, white);
+        if (!(w > trl)) break;
+        if (w >= Fc) {
+          ii = j;
+          Fc = w;
+        }
+      }
+      const int slot = atomicAdd(ncand, 1);
+      if (slot < cap) {
+        DevCand dcnd;
+        dcnd.task = task;
+        dcnd.ss = ss0 + sidx;
+        dcnd.ii = ii + nmin;
+        dcnd.pad = 0;
+        dcnd.F = (double)Fc;
+        cand[slot] = dcnd;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------
+// engine
+
+inline Geom make_geom(int L, int E) {
+  Geom g;
+  int m = 0;
+  while ((1 << m) < L) ++m;
+  g.L = L;
+  g.logL = m;
+  g.logL1 = (m + 1) / 2;
+  g.logL2 = m / 2;
+  g.L1 = 1 << g.logL1;
+  g.L2 = 1 << g.logL2;
+  int logE = 0;
+  while ((1 << logE) < E) ++logE;
+  g.logC = logE - 1 - g.logL1;
+  g.C = 1 << g.logC;
+  g.logRr = logE - 1 - g.logL2;
+  g.Rr = 1 << g.logRr;
+  g.twlo_log = 10;
+  return g;
+}
+
+template <typename R, int PM> class EngineT : public Engine {
+  typedef typename CT<R>::T T;
+  Buffers b_;
+  Geom gf_, gi_, gm_;
+  long long launches_ = 0;
+
+  // opt-in above 48 KB of dynamic shared memory, once per kernel instance
+  template <class K> static void smem_attr(K kernel, int bytes, bool& done) {
+    if (!done) {
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      done = true;
+    }
+  }
+
+  template <int SIGN, class Loader, class Storer>
+  cudaError_t fft(const Geom& g, const void* const* tw, const Loader& ld, const Storer& st, int batch,
+                  cudaStream_t stream) {
+    constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
+    const T* t1 = (const T*)tw[0];
+    const T* t2 = (const T*)tw[1];
+    const T* tlo = (const T*)tw[2];
+    const T* thi = (const T*)tw[3];
+    T* yb = (T*)b_.ybuf;
+    const int smA = (E + g.L1) * (int)sizeof(T) + 128;
+    const int smB = (E + g.L2) * (int)sizeof(T);
+    auto ka = k_pass_a<R, SIGN, Loader>;
+    auto kb = k_pass_b<R, SIGN, Storer>;
+    static bool doneA = false, doneB = false;
+    smem_attr(ka, (E + 1024) * (int)sizeof(T) + 128, doneA);
+    smem_attr(kb, (E + 1024) * (int)sizeof(T), doneB);
+    dim3 ga(g.L2 >> g.logC, batch), gb(g.L1 >> g.logRr, batch);
+    ka<<<ga, NT, smA, stream>>>(ld, g, t1, tlo, thi, yb);
+    kb<<<gb, NT, smB, stream>>>(st, g, t2, yb);
+    launches_ += 2;
+    return cudaGetLastError();
+  }
+
+ public:
+  explicit EngineT(const Buffers& b) : b_(b) {
+    gf_ = make_geom(b.nfft, TileCfg<R>::E);
+    gi_ = make_geom(b.Ninterp, TileCfg<R>::E);
+    gm_ = make_geom(b.nfftf, TileCfg<R>::E);
+  }
+
+  long long launches() const override { return launches_; }
+  size_t real_size() const override { return sizeof(R); }
+
+  cudaError_t prelude(const SkyArgs& sky, cudaStream_t st) override {
+    const int N = b_.N, nifo = b_.nifo;
+    const int nbx = (N + 255) / 256;
+    k_prelude_mod<R, PM><<<dim3(nbx, nifo), 256, 0, st>>>(
+        b_.xDat, b_.DetSSB, (const R*)b_.cosmodf, (const R*)b_.sinmodf, b_.dc, sky, N, (T*)b_.xin,
+        b_.shftf, b_.ph0, b_.ph1, b_.part);
+    k_prelude_sums<<<1, 32, 0, st>>>(b_.part, nbx, nifo, b_.dc, b_.sums);
+    launches_ += 2;
+    // forward FFT of the zero-padded series (length nfft)
+    PlainLoader<R> pl{(const T*)b_.xin, N, N};
+    CStore<R> cs1{(T*)b_.spec, b_.nfft, (R)1};
+    cudaError_t e = fft<-1>(gf_, b_.tw_fwd, pl, cs1, nifo, st);
+    if (e != cudaSuccess) return e;
+    // spectrum remap + backward FFT (length Ninterp), scale interpftpad/Ninterp
+    RemapLoader<R> rl{(const T*)b_.spec, b_.nfft, b_.nfft / 2 + 1, b_.Ninterp - b_.nfft};
+    CStore<R> cs2{(T*)b_.yint, b_.Ninterp, (R)(2.0 / b_.Ninterp)};
+    e = fft<+1>(gi_, b_.tw_inv, rl, cs2, nifo, st);
+    if (e != cudaSuccess) return e;
+    // spline through the first 2N points of each resampled array
+    const int n = 2 * N;
+    const int nch = (n + kSplineChunk - 1) / kSplineChunk;
+    const int nthr = nch * 2 * nifo;
+    k_spline_fwd<R><<<(nthr + 127) / 128, 128, 0, st>>>((const T*)b_.yint, b_.Ninterp, (double2*)b_.u,
+                                                        n, nch, 2 * nifo, b_.spline_invp);
+    k_spline_bwd<R><<<(nthr + 127) / 128, 128, 0, st>>>((const double2*)b_.u, (T*)b_.y2, n, nch,
+                                                        2 * nifo, b_.spline_p);
+    k_splint<R><<<dim3(nbx, nifo), 256, 0, st>>>((const T*)b_.yint, b_.Ninterp, (const T*)b_.y2,
+                                                 b_.shftf, b_.dc, N, (T*)b_.xm);
+    launches_ += 3;
+    return cudaGetLastError();
+  }
+
+  cudaError_t spindowns(const SkyArgs& sky, int ss0, int nb, double trl, int white, int s0_flag,
+                        cudaStream_t st, void* Fdbg) override {
+    SpinLoader<R, PM> sl;
+    sl.xm = (const T*)b_.xm;
+    sl.ph0 = b_.ph0;
+    sl.ph1 = b_.ph1;
+    sl.N = b_.N;
+    sl.nifo = b_.nifo;
+    sl.ss0 = ss0;
+    sl.s0_flag = s0_flag;
+    sl.M0 = sky.M0;
+    sl.M4 = sky.M4;
+    sl.M5 = sky.M5;
+    sl.s1_0 = sky.s1_0;
+    FstatStore<R> fs{(R*)b_.F, b_.sums, b_.nmin, b_.nmax, b_.bins};
+    cudaError_t e = fft<-1>(gm_, b_.tw_main, sl, fs, nb, st);
+    if (e != cudaSuccess) return e;
+    if (b_.nblk > 0 && !white) {
+      k_blockmean<R><<<dim3(b_.nblk, nb), 256, 0, st>>>((const R*)b_.F, b_.bins, b_.nblk, (R*)b_.mu);
+      launches_ += 1;
+    }
+    const int nchunk = (b_.bins + 4095) / 4096;
+    k_threshold<R><<<dim3(nchunk, nb), 256, 0, st>>>((const R*)b_.F, b_.bins, b_.nblk, (const R*)b_.mu,
+                                                     white, (R)trl, b_.nmin, ss0, sky.task, b_.cand,
+                                                     b_.ncand, b_.cand_cap, (R*)Fdbg);
+    launches_ += 1;
+    return cudaGetLastError();
+  }
+};
+
+}  // namespace pa

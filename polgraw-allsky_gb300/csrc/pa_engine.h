@@ -1,0 +1,99 @@
+// pa_engine.h -- host-side interface between the C-ABI layer (pa_api.cu) and
+// the templated device engines (pa_engine_f32.cu, pa_engine_f64.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pa {
+
+constexpr int kMaxDet = 8;
+
+// Per-context constants of one detector (uploaded once).
+struct DetConst {
+  double amod[9];
+  double sig2, inv_sig2;
+  double sphir, cphir;
+};
+
+// Per-sky-point scalars, computed on the host in FP64 exactly as
+// job_core() does (jobcore.c:243-299) and passed by value to the kernels.
+struct SkyArgs {
+  double het0;            // fmod(nn M8 + mm M12, M0)
+  double oms;
+  double sinal, cosal, sindel, cosdel;
+  double nS[3];           // unit vector to the source
+  double shft1[kMaxDet];  // nS . DetSSB[0..2] per detector
+  double cosalfr[kMaxDet], sinalfr[kMaxDet];  // modvir rotated angles
+  double s1_0;            // nn M9 + mm M13 (0 with --nospindown)
+  double M5;              // spindown step (0 with --nospindown)
+  double M0, M4;          // frequency step, het1 step
+  int task;               // index of the sky point in the current batch
+};
+
+// One candidate found on the device (frequency bin ii is absolute).
+struct DevCand {
+  int task, ss, ii, pad;
+  double F;
+};
+
+// Device buffers owned by the context and shared with the engine.
+struct Buffers {
+  int N, nfft, Ninterp, nfftf, nmin, nmax, bins, nblk, nifo, fftpad;
+  int sbatch;                       // spindowns per fused launch
+  const double* xDat;               // [nifo][N]
+  const double* DetSSB;             // [nifo][3N]
+  const void* cosmodf;              // [N] Real
+  const void* sinmodf;              // [N] Real
+  const DetConst* dc;               // [nifo]
+  const double* spline_invp;        // [64] pivots 2/(p+4) of the spline solve
+  const double* spline_p;           // [64] p_i
+  void* xin;                        // [nifo][2][N] Real complex
+  void* spec;                       // [nifo][2][nfft]
+  void* yint;                       // [nifo][2][Ninterp]
+  double* u;                        // [nifo][2][2N] double2
+  void* y2;                         // [nifo][2][2N] Real complex
+  double* shftf;                    // [nifo][N]
+  void* ph0;                        // phase coefficients [nifo][N] (mode dependent)
+  void* ph1;
+  void* xm;                         // [nifo][2][N] Real complex
+  double* part;                     // partial sums of a^2, b^2
+  double* sums;                     // aa, bb, 1/aa, 1/bb
+  void* ybuf;                       // FFT intermediate, max(sbatch*2*nfftf, nifo*2*Ninterp)
+  void* F;                          // [sbatch][bins] Real
+  void* mu;                         // [sbatch][nblk] Real
+  DevCand* cand;
+  int* ncand;
+  int cand_cap;
+  // twiddle tables (Real complex) per transform
+  const void* tw_fwd[4];            // nfft forward: tw1, tw2, twlo, twhi
+  const void* tw_inv[4];            // Ninterp backward
+  const void* tw_main[4];           // nfftf forward
+};
+
+class Engine {
+ public:
+  virtual ~Engine() {}
+  // Enqueues the per-sky prelude (jobcore.c:270-393) on `st`.
+  virtual cudaError_t prelude(const SkyArgs& sky, cudaStream_t st) = 0;
+  // Enqueues spindowns ss0 .. ss0+nb-1 (nb <= sbatch): phase modulation,
+  // FFT, F-statistic, normalisation, threshold and candidate compaction.
+  // Fdbg (optional): normalised F of the batch, [nb][bins] Real.
+  virtual cudaError_t spindowns(const SkyArgs& sky, int ss0, int nb, double trl, int white,
+                                int s0_flag, cudaStream_t st, void* Fdbg) = 0;
+  virtual long long launches() const = 0;
+  virtual size_t real_size() const = 0;
+};
+
+// Factories (defined in the per-precision translation units).
+Engine* make_engine_f32(const Buffers& b, int phase_mode);
+Engine* make_engine_f64(const Buffers& b);
+
+// Phase-coefficient bytes per sample for a (precision, phase mode).
+inline size_t phase_bytes(int fp64, int phase_mode, int which) {
+  if (fp64) return which == 0 ? 8 : 0;
+  if (phase_mode == 1) return 8;          // fixed: A and B (u64 each)
+  if (phase_mode == 2) return which == 0 ? 8 : 0;  // float-float
+  return which == 0 ? 8 : 0;              // FP64 tmp1
+}
+
+}  // namespace pa

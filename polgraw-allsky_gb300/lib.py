@@ -1,0 +1,324 @@
+"""ctypes binding of libpolgraw_gb300.so (include/polgraw_gb300.h and
+include/polgraw_gb300_host.h).
+
+This is the Python-side mirror that the tests and bench.py use to call the
+C-ABI exactly as a C caller of job_core() would: plain structs, host
+buffers, status codes.  The CUDA path is the only implementation behind it;
+if the library or a GPU is missing the calls fail loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpolgraw_gb300.so")
+
+PA_OK, PA_ERR_ARG, PA_ERR_CUDA, PA_ERR_CAPACITY, PA_ERR_TIMEOUT, PA_ERR_NOMEM, PA_ERR_NODEV = range(7)
+PA_PREC_MIXED, PA_PREC_FP64 = 0, 1
+PA_PHASE_F64, PA_PHASE_FIXED, PA_PHASE_FF = 0, 1, 2
+PA_NPAR = 5
+PHASE_NAMES = {"f64": PA_PHASE_F64, "fixed": PA_PHASE_FIXED, "ff": PA_PHASE_FF}
+
+# Every exported entry point declared in include/*.h
+EXPORTS = [
+    "pa_version", "pa_device_count", "pa_create", "pa_set_data", "pa_destroy", "pa_last_error",
+    "pa_job_core", "pa_search_batch", "pa_debug_prelude", "pa_debug_fstat", "pa_kernel_launches",
+    "pa_host_create", "pa_host_setup", "pa_host_search", "pa_host_main", "pa_host_destroy",
+    "pa_host_settings", "pa_host_detectors", "pa_host_range", "pa_host_core_opts",
+    "pa_host_config", "pa_host_detector_name",
+]
+
+
+class Settings(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("fpo", "dt", "B", "oms", "omr", "Smin", "Smax", "sepsm", "cepsm")] + \
+               [(n, C.c_int) for n in ("nfft", "nod", "N", "nfftf", "nmax", "nmin", "s", "nd",
+                                       "interpftpad", "fftpad", "Ninterp", "nifo")] + \
+               [("M", C.c_double * 16), ("numlines_band", C.c_int), ("lines", C.POINTER(C.c_double))]
+
+
+class Detector(C.Structure):
+    _fields_ = [("xDat", C.POINTER(C.c_double)), ("DetSSB", C.POINTER(C.c_double)),
+                ("sig2", C.c_double), ("sphir", C.c_double), ("cphir", C.c_double),
+                ("amod", C.c_double * 9)]
+
+
+class Opts(C.Structure):
+    _fields_ = [("trl", C.c_double), ("white_flag", C.c_int), ("s0_flag", C.c_int), ("use_range", C.c_int)]
+
+
+class Range(C.Structure):
+    _fields_ = [("pmr", C.c_int * 2), ("mr", C.c_int * 2), ("nr", C.c_int * 2), ("spndr", C.c_int * 2),
+                ("pst", C.c_int), ("mst", C.c_int), ("nst", C.c_int), ("sst", C.c_int)]
+
+
+class CandIdx(C.Structure):
+    _fields_ = [("pm", C.c_int), ("mm", C.c_int), ("nn", C.c_int), ("ss", C.c_int), ("ii", C.c_int),
+                ("F", C.c_float)]
+
+
+class Config(C.Structure):
+    _fields_ = [("precision", C.c_int), ("phase_mode", C.c_int), ("spindown_batch", C.c_int), ("device", C.c_int)]
+
+
+class Sky(C.Structure):
+    _fields_ = [("pm", C.c_int), ("mm", C.c_int), ("nn", C.c_int)]
+
+
+_lib = None
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Loads the library (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        from . import build as _b
+        _b.build()
+    lib = C.CDLL(p)
+    P = C.POINTER
+    lib.pa_version.restype = C.c_char_p
+    lib.pa_device_count.restype = C.c_int
+    lib.pa_create.restype = C.c_void_p
+    lib.pa_create.argtypes = [P(Settings), P(Detector), C.c_int, P(Config), P(C.c_int)]
+    lib.pa_set_data.argtypes = [C.c_void_p, P(Detector), C.c_int]
+    lib.pa_destroy.argtypes = [C.c_void_p]
+    lib.pa_destroy.restype = None
+    lib.pa_last_error.restype = C.c_char_p
+    lib.pa_last_error.argtypes = [C.c_void_p]
+    lib.pa_job_core.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P(Opts), P(Range), P(C.c_int),
+                                P(C.c_double), C.c_int, P(CandIdx), P(C.c_int), P(C.c_int)]
+    lib.pa_search_batch.argtypes = [C.c_void_p, P(Sky), C.c_int, P(Opts), P(Range), P(C.c_int),
+                                    P(C.c_double), C.c_int, P(CandIdx), P(C.c_int), P(C.c_int)]
+    lib.pa_debug_prelude.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, P(C.c_double), P(C.c_double),
+                                     P(C.c_double), P(C.c_double)]
+    lib.pa_debug_fstat.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, P(Opts), P(C.c_double)]
+    lib.pa_kernel_launches.restype = C.c_longlong
+    lib.pa_kernel_launches.argtypes = [C.c_void_p]
+    lib.pa_host_create.restype = C.c_void_p
+    lib.pa_host_create.argtypes = [C.c_int, P(C.c_char_p), P(C.c_int)]
+    lib.pa_host_setup.argtypes = [C.c_void_p]
+    lib.pa_host_search.argtypes = [C.c_void_p, C.c_void_p]
+    lib.pa_host_main.argtypes = [C.c_int, P(C.c_char_p)]
+    lib.pa_host_destroy.argtypes = [C.c_void_p]
+    lib.pa_host_destroy.restype = None
+    lib.pa_host_settings.restype = P(Settings)
+    lib.pa_host_settings.argtypes = [C.c_void_p]
+    lib.pa_host_detectors.restype = P(Detector)
+    lib.pa_host_detectors.argtypes = [C.c_void_p, P(C.c_int)]
+    lib.pa_host_range.restype = P(Range)
+    lib.pa_host_range.argtypes = [C.c_void_p]
+    lib.pa_host_core_opts.argtypes = [C.c_void_p, P(Opts)]
+    lib.pa_host_core_opts.restype = None
+    lib.pa_host_config.argtypes = [C.c_void_p, P(Config)]
+    lib.pa_host_config.restype = None
+    lib.pa_host_detector_name.restype = C.c_char_p
+    lib.pa_host_detector_name.argtypes = [C.c_void_p, C.c_int]
+    _lib = lib
+    return lib
+
+
+def _argv(args: list[str]):
+    arr = (C.c_char_p * (len(args) + 1))()
+    arr[:-1] = [a.encode() for a in args]
+    arr[-1] = None
+    return arr
+
+
+class Host:
+    """Search set-up exactly as the drop-in program does it (handle_opts ...
+    read_checkpoints), from a reference-style command line."""
+
+    def __init__(self, args: list[str]):
+        self.lib = load()
+        argv = ["gwsearch-gb300"] + list(args)
+        self._argv = _argv(argv)
+        rc = C.c_int(0)
+        h = self.lib.pa_host_create(len(argv), self._argv, C.byref(rc))
+        if not h:
+            raise RuntimeError("pa_host_create failed (%d)" % rc.value)
+        self.h = h
+        self.setup_rc = self.lib.pa_host_setup(h)
+        if self.setup_rc == 101:
+            raise RuntimeError("pa_host_setup failed")
+
+    @property
+    def settings(self) -> Settings:
+        return self.lib.pa_host_settings(self.h).contents
+
+    def detectors(self):
+        n = C.c_int(0)
+        p = self.lib.pa_host_detectors(self.h, C.byref(n))
+        return p, n.value
+
+    @property
+    def range(self) -> Range:
+        return self.lib.pa_host_range(self.h).contents
+
+    def opts(self) -> Opts:
+        o = Opts()
+        self.lib.pa_host_core_opts(self.h, C.byref(o))
+        return o
+
+    def config(self) -> Config:
+        c = Config()
+        self.lib.pa_host_config(self.h, C.byref(c))
+        return c
+
+    def sky_points(self) -> list[tuple[int, int, int]]:
+        """(pm, mm, nn) in the sky-loop order (jobcore.c:90-98)."""
+        r = self.range
+        out = []
+        mst, nst = r.mst, r.nst
+        for pm in range(r.pst, r.pmr[1] + 1):
+            for mm in range(mst, r.mr[1] + 1):
+                for nn in range(nst, r.nr[1] + 1):
+                    out.append((pm, mm, nn))
+                nst = r.nr[0]
+            mst = r.mr[0]
+        return out
+
+    def close(self):
+        if self.h:
+            self.lib.pa_host_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SearchError(RuntimeError):
+    pass
+
+
+class Context:
+    """A pa_ctx: GPU search context for one set of inputs."""
+
+    def __init__(self, settings: Settings, dets, nifo: int, precision: int = PA_PREC_MIXED,
+                 phase_mode: int = PA_PHASE_FIXED, spindown_batch: int = 0, device: int = 0):
+        self.lib = load()
+        self.cfg = Config(precision, phase_mode, spindown_batch, device)
+        st = C.c_int(0)
+        self.ctx = self.lib.pa_create(C.byref(settings), dets, nifo, C.byref(self.cfg), C.byref(st))
+        if not self.ctx:
+            raise SearchError("pa_create failed (%d): %s" % (st.value, self.lib.pa_last_error(None).decode()))
+        self.settings = settings
+        self.nifo = nifo
+
+    def error(self) -> str:
+        return self.lib.pa_last_error(self.ctx).decode()
+
+    def job_core(self, pm, mm, nn, opts: Opts, rng: Range, cap: int = 1 << 16):
+        """Returns (records [n,5], idx structured array, FNum increment)."""
+        sgnlc = C.c_int(0)
+        fnum = C.c_int(0)
+        needed = C.c_int(0)
+        while True:
+            buf = np.zeros((cap, PA_NPAR))
+            idx = (CandIdx * cap)()
+            rc = self.lib.pa_job_core(self.ctx, pm, mm, nn, C.byref(opts), C.byref(rng), C.byref(sgnlc),
+                                      buf.ctypes.data_as(C.POINTER(C.c_double)), cap, idx, C.byref(fnum),
+                                      C.byref(needed))
+            if rc == PA_ERR_CAPACITY:
+                cap = needed.value + 16
+                continue
+            if rc != PA_OK:
+                raise SearchError("pa_job_core failed (%d): %s" % (rc, self.error()))
+            break
+        n = sgnlc.value
+        return buf[:n].copy(), idx_to_array(idx, n), fnum.value
+
+    def search_batch(self, tasks, opts: Opts, rng: Range, cap: int = 1 << 18):
+        arr = (Sky * len(tasks))(*[Sky(*t) for t in tasks])
+        sgnlc = C.c_int(0)
+        fnum = C.c_int(0)
+        needed = C.c_int(0)
+        while True:
+            buf = np.zeros((cap, PA_NPAR))
+            idx = (CandIdx * cap)()
+            rc = self.lib.pa_search_batch(self.ctx, arr, len(tasks), C.byref(opts), C.byref(rng),
+                                          C.byref(sgnlc), buf.ctypes.data_as(C.POINTER(C.c_double)), cap, idx,
+                                          C.byref(fnum), C.byref(needed))
+            if rc == PA_ERR_CAPACITY:
+                cap = needed.value + 16
+                continue
+            if rc != PA_OK:
+                raise SearchError("pa_search_batch failed (%d): %s" % (rc, self.error()))
+            break
+        n = sgnlc.value
+        return buf[:n].copy(), idx_to_array(idx, n), fnum.value
+
+    def prelude(self, pm, mm, nn):
+        N = self.settings.N
+        xa = np.zeros((self.nifo, N), dtype=np.complex128)
+        xb = np.zeros_like(xa)
+        aa = C.c_double(0)
+        bb = C.c_double(0)
+        rc = self.lib.pa_debug_prelude(self.ctx, pm, mm, nn, xa.ctypes.data_as(C.POINTER(C.c_double)),
+                                       xb.ctypes.data_as(C.POINTER(C.c_double)), C.byref(aa), C.byref(bb))
+        if rc != PA_OK:
+            raise SearchError("pa_debug_prelude failed (%d): %s" % (rc, self.error()))
+        return xa, xb, aa.value, bb.value
+
+    def fstat(self, pm, mm, nn, ss, opts: Opts):
+        F = np.zeros(self.settings.nmax - self.settings.nmin)
+        rc = self.lib.pa_debug_fstat(self.ctx, pm, mm, nn, ss, C.byref(opts),
+                                     F.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != PA_OK:
+            raise SearchError("pa_debug_fstat failed (%d): %s" % (rc, self.error()))
+        return F
+
+    def set_data(self, dets, nifo):
+        rc = self.lib.pa_set_data(self.ctx, dets, nifo)
+        if rc != PA_OK:
+            raise SearchError("pa_set_data failed (%d): %s" % (rc, self.error()))
+
+    def launches(self) -> int:
+        return int(self.lib.pa_kernel_launches(self.ctx))
+
+    def close(self):
+        if self.ctx:
+            self.lib.pa_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+IDX_DTYPE = np.dtype([("pm", "i4"), ("mm", "i4"), ("nn", "i4"), ("ss", "i4"), ("ii", "i4"), ("F", "f4")])
+
+
+def idx_to_array(idx, n: int) -> np.ndarray:
+    raw = np.frombuffer(C.string_at(C.addressof(idx), n * C.sizeof(CandIdx)), dtype=IDX_DTYPE) if n else \
+        np.zeros(0, dtype=IDX_DTYPE)
+    return raw.copy()
+
+
+def make_detectors(xdats, detssbs, sig2s, sphirs, cphirs, amods):
+    """Builds a pa_detector array from numpy inputs (arrays are kept alive by
+    the returned tuple)."""
+    n = len(xdats)
+    arr = (Detector * n)()
+    keep = []
+    for i in range(n):
+        x = np.ascontiguousarray(xdats[i], dtype=np.float64)
+        d = np.ascontiguousarray(detssbs[i], dtype=np.float64)
+        keep += [x, d]
+        arr[i].xDat = x.ctypes.data_as(C.POINTER(C.c_double))
+        arr[i].DetSSB = d.ctypes.data_as(C.POINTER(C.c_double))
+        arr[i].sig2 = sig2s[i]
+        arr[i].sphir = sphirs[i]
+        arr[i].cphir = cphirs[i]
+        for k in range(9):
+            arr[i].amod[k] = amods[i][k]
+    return arr, keep
