@@ -1,0 +1,335 @@
+"""Benchmark of the coherent-search hot path (job_core) on one GB300.
+
+Workload (the H1+L1 network configuration): two detectors, N = 86164
+samples at dt = 2 s (2 sidereal days), nfft = 131072, fftpad = 1,
+interpftpad = 2, Gaussian-like noise sigma 1.0 (H1) and 1.3 (L1), five
+injected signals (SNR 8-15, seed 2002), ~2000 sky points on the lattice of
+one hemisphere x 200 spindowns.  Inputs are synthetic (deterministic
+generator polgraw_gb300.synth); no dataset is read.
+
+A step is one pass of the search over the sky points (pa_search_batch via
+the C-ABI).  `value` = templates (sky x spindown x frequency bin) per second
+with the inputs resident in HBM, timed with CUDA events on the context's
+stream; `e2e` = the same metric through the C-ABI with host buffers, the
+host->device upload of the data and the device->host candidates inside the
+timed region.  The L2 is flushed (256 MB write) before every timed step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib.util
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+
+
+def load_package():
+    name = "polgraw_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    d = os.path.join(ROOT, "polgraw-allsky_gb300")
+    spec = importlib.util.spec_from_file_location(name, os.path.join(d, "__init__.py"),
+                                                  submodule_search_locations=[d])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+load_package()
+from polgraw_gb300 import synth  # noqa: E402
+
+METRIC = "templates/sec (sky x spindown x bin) mixed vs all-FP64 on GB300 at 1e-4 F-stat err"
+UNIT = "templates/s"
+WORKLOAD = "network H1+L1, N=86164 dt=2s, nfft=131072, 2000 sky x 200 spindowns, 5 injections"
+NSKY_DEFAULT = 2000
+NSPIN_DEFAULT = 200
+
+
+def make_workload(root: str, nspin: int):
+    """Writes the data set and returns the search command line."""
+    dt, nod, band = 2.0, 2, 666
+    N = synth.nsamples(nod, dt)
+    probe = synth.Dataset(root=root, ident=1, band=band, dt=dt, nod=nod, fftpad=1, M=[], dets=["H1", "L1"], N=N)
+    oms = probe.oms
+    spacing = oms * math.sqrt(math.pi / 2000.)
+    M = synth.grid_matrix(probe.nfft, oms, m5=-1e-9, sky=(spacing, 0.0, 0.0, spacing))
+    ds = synth.write_dataset(root, ident=1, band=band, dt=dt, nod=nod, fftpad=1, dets=["H1", "L1"], M=M)
+    rng = np.random.default_rng(2002)
+    for k in range(5):
+        # uniform in band and spindown range, sky on the first hemisphere
+        while True:
+            delta = float(rng.uniform(-1.2, 1.2))
+            alpha = float(rng.uniform(0, 2 * math.pi))
+            _, pm = synth.ast2lin(alpha, delta)
+            if pm == 1:
+                break
+        synth.inject(ds, f=float(rng.uniform(0.2, 2.9)), fdot=float(rng.uniform(-1.9e-7, 0.0)),
+                     delta=delta, alpha=alpha, snr=float(rng.uniform(8, 15)))
+    nmax = int(math.ceil(1.0 / math.sqrt(math.pi / 2000.))) + 1
+    rpath = os.path.join(root, "range.txt")
+    synth.write_range(rpath, [0, nspin - 1], [-nmax, nmax], [-nmax, nmax], [1, 1])
+    return ["-data", root, "-ident", "1", "-band", str(band), "-dt", "2", "-nod", str(nod), "-range", rpath,
+            "-output", os.path.join(root, "out"), "--nocheckpoint"]
+
+
+def sky_tasks(host, limit: int):
+    s = host.settings
+    out = []
+    for (pm, mm, nn) in host.sky_points():
+        al1 = nn * s.M[10] + mm * s.M[14]
+        al2 = nn * s.M[11] + mm * s.M[15]
+        if (al1 * al1 + al2 * al2) / (s.oms * s.oms) <= 1.0:
+            out.append((pm, mm, nn))
+    return out[:limit]
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, reasons)."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.p = None
+        self.path = tempfile.mktemp(suffix=".csv")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def l2_flush():
+    import torch
+    buf = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    buf.zero_()
+    torch.cuda.synchronize()
+    del buf
+
+
+def peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def cpu_baseline(host, tasks, nsky_sample: int, nthreads: int):
+    """The CPU oracle (all-FP64 C restatement, OpenMP over spindowns) on a
+    bounded sample of the same sky points: templates/s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import Oracle
+    dets, nifo = host.detectors()
+    orc = Oracle(host.settings, dets, nifo, nthreads=nthreads)
+    opts, rng = host.opts(), host.range
+    s = host.settings
+    bins = s.nmax - s.nmin
+    nspin = rng.spndr[1] - rng.spndr[0] + 1
+    sample = tasks[:nsky_sample]
+    t0 = time.perf_counter()
+    for (pm, mm, nn) in sample:
+        rng.sst = rng.spndr[0]
+        orc.job_core(pm, mm, nn, opts, rng)
+    dt = time.perf_counter() - t0
+    orc.close()
+    return len(sample) * nspin * bins / dt, dt, len(sample)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sky", type=int, default=NSKY_DEFAULT)
+    ap.add_argument("--spindowns", type=int, default=NSPIN_DEFAULT)
+    ap.add_argument("--phase", default="fixed", choices=["fixed", "f64", "ff"])
+    ap.add_argument("--fp64-sky", type=int, default=48, help="sky points timed in the all-FP64 form")
+    ap.add_argument("--cpu-sky", type=int, default=2, help="sky points in the CPU-baseline sample")
+    ap.add_argument("--no-extras", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from polgraw_gb300 import build as pbuild, lib as L
+    pbuild.build()
+    tmp = tempfile.mkdtemp(prefix="pa_bench_")
+    argv = make_workload(tmp, args.spindowns)
+    host = L.Host(argv)
+    tasks = sky_tasks(host, args.sky)
+    s = host.settings
+    bins = s.nmax - s.nmin
+    nspin = args.spindowns
+    cfg = {"workload": WORKLOAD, "sky_points": len(tasks), "spindowns": nspin, "bins": bins,
+           "nifo": 2, "N": s.N, "nfftf": s.nfftf, "phase": args.phase,
+           "l2": "flushed (256 MB write) before each timed step", "parallelism": "replicas" if world > 1 else "1 GPU"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        nth = os.cpu_count() or 1
+        vals = []
+        for _ in range(args.warmup if args.warmup < 1 else 1):
+            cpu_baseline(host, tasks, 1, nth)
+        t_all = 0.0
+        ntempl = 0
+        for _ in range(args.steps):
+            v, dt, ns = cpu_baseline(host, tasks, args.cpu_sky, nth)
+            vals.append(v)
+            t_all += dt
+            ntempl += ns * nspin * bins
+        value = ntempl / t_all
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": cfg,
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
+                                 "sample": "%d sky points x %d spindowns per step (CPU oracle, OpenMP)" %
+                                           (args.cpu_sky, nspin)},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        tasks = tasks[rank::world]
+    dets, nifo = host.detectors()
+    phase = L.PHASE_NAMES[args.phase]
+    ctx = L.Context(s, dets, nifo, precision=L.PA_PREC_MIXED, phase_mode=phase, device=0)
+    opts, rng = host.opts(), host.range
+    templates = len(tasks) * nspin * bins
+    for _ in range(args.warmup):
+        ctx.search_batch(tasks, opts, rng)
+    launches0 = ctx.launches()
+    clocks = ClockSampler(0)
+    dev_ms = []
+    ncand = 0
+    for _ in range(args.steps):
+        l2_flush()
+        rec, idx, fnum = ctx.search_batch(tasks, opts, rng)
+        dev_ms.append(ctx.last_call_ms())
+        ncand = len(rec)
+    clk = clocks.stop()
+    launches = (ctx.launches() - launches0) // max(1, args.steps)
+    t_dev = sum(dev_ms) / 1e3
+    value = templates * args.steps / t_dev
+
+    # end to end: host buffers in, candidates out, through the C-ABI
+    e2e_t = 0.0
+    for _ in range(args.steps):
+        l2_flush()
+        t0 = time.perf_counter()
+        ctx.set_data(dets, nifo)
+        rec, idx, fnum = ctx.search_batch(tasks, opts, rng)
+        e2e_t += time.perf_counter() - t0
+    e2e = templates * args.steps / e2e_t
+    h2d = nifo * s.N * 8 * 4
+    d2h = 4 + len(rec) * 24
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64phase", "data": "synthetic", "config": cfg,
+           "clocks": clk, "gpu_launches": int(launches),
+           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "candidates_per_step": ncand}
+
+    if not args.no_extras:
+        # per-kernel CUDA-event profile of one step (not the timed number)
+        ctx.set_profiling(True)
+        ctx.profile_reset()
+        l2_flush()
+        ctx.search_batch(tasks, opts, rng)
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        tot = sum(v[0] for v in prof.values())
+        top = max(prof.items(), key=lambda kv: kv[1][0])
+        name, (ms, nl, items) = top
+        pk = peaks()
+        # algorithmic bytes of the spindown loop: xDatm{a,b} (2 x 8 B FP32
+        # complex) + one 8-B phase coefficient per detector and sample
+        per_unit = nifo * s.N * 24
+        achieved = per_unit * items / (ms / 1e3) / 1e9 if name == "spindown_pass_a" else None
+        out["roofline"] = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": pk["hbm_gbs"],
+                           "unit": "GB/s", "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
+                           "traffic": None, "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
+                           "avg_launch_ms": ms / max(1, nl), "units_per_launch": items / max(1, nl)}
+        out["kernel_share"] = {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+
+        # all-FP64 form of the same kernels on a subset, and candidate agreement
+        sub = tasks[:args.fp64_sky]
+        c64 = L.Context(s, dets, nifo, precision=L.PA_PREC_FP64, device=0)
+        c64.search_batch(sub[:2], opts, rng)
+        l2_flush()
+        r64, i64, _ = c64.search_batch(sub, opts, rng)
+        ms64 = c64.last_call_ms()
+        v64 = len(sub) * nspin * bins / (ms64 / 1e3)
+        rmx, imx, _ = ctx.search_batch(sub, opts, rng)
+        msmx = ctx.last_call_ms()
+        vmx = len(sub) * nspin * bins / (msmx / 1e3)
+        k64 = {tuple(int(x[f]) for f in ("pm", "mm", "nn", "ss", "ii")): r[4] for x, r in zip(i64, r64)}
+        kmx = {tuple(int(x[f]) for f in ("pm", "mm", "nn", "ss", "ii")): r[4] for x, r in zip(imx, rmx)}
+        F = lambda snr: snr * snr / 2 + 2  # noqa: E731
+        common = [k for k in k64 if k in kmx]
+        err = max([abs(F(kmx[k]) - F(k64[k])) / F(k64[k]) for k in common], default=0.0)
+        edge = lambda k, d: abs(F(d[k]) - opts.trl) <= 1e-4 * opts.trl  # noqa: E731
+        only64 = [k for k in k64 if k not in kmx and not edge(k, k64)]
+        onlymx = [k for k in kmx if k not in k64 and not edge(k, kmx)]
+        out["fp64_form"] = {"value": v64, "unit": UNIT, "sky_points": len(sub), "mixed_same_subset": vmx,
+                            "mixed_over_fp64": vmx / v64, "fstat_rel_err_max": err,
+                            "candidates": len(k64), "index_mismatches": len(only64) + len(onlymx)}
+        c64.close()
+        if rank == 0:
+            nth = os.cpu_count() or 1
+            cv, cdt, cn = cpu_baseline(host, tasks, args.cpu_sky, nth)
+            out["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": nth, "kind": "port",
+                                   "sample": "%d sky points x %d spindowns (CPU oracle, OpenMP, %.1f s)" %
+                                             (cn, nspin, cdt)}
+    if rank == 0:
+        print(json.dumps(out))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -159,8 +159,10 @@ int pa_job_core(pa_ctx *ctx, int pm, int mm, int nn, const pa_opts *opts,
 /* Batched form of the sky loop body: runs job_core() for ntasks sky points
  * with the work of several sky points in flight, then appends all records in
  * task order (each task's records in serial order).  Same buffer contract
- * as pa_job_core().  The spindown range per task follows the same rules
- * (s_range->sst is used for every task when opts->use_range is set). */
+ * as pa_job_core().  The spindown range per task follows the same rules;
+ * with opts->use_range the first task starts at s_range->sst and later
+ * tasks at s_range->spndr[0], as the sky loop resets sst after each sky
+ * point (jobcore.c:123). */
 int pa_search_batch(pa_ctx *ctx, const pa_sky *tasks, int ntasks,
                     const pa_opts *opts, const pa_range *s_range, int *sgnlc,
                     double *sgnlv, int sgnlv_cap, pa_cand_idx *idx, int *FNum,
@@ -182,6 +184,23 @@ int pa_debug_fstat(pa_ctx *ctx, int pm, int mm, int nn, int ss,
 
 /* Number of CUDA kernel launches issued by this context so far. */
 long long pa_kernel_launches(const pa_ctx *ctx);
+
+/* Device time in milliseconds of the last pa_job_core/pa_search_batch call,
+ * from CUDA events recorded on the context's stream before its first and
+ * after its last kernel (the reference's analogue is the wall-clock
+ * "Time elapsed" of jobcore.c:178-182). */
+double pa_last_call_ms(const pa_ctx *ctx);
+
+/* Per-kernel profile: when on, every kernel launch of the context is
+ * bracketed by CUDA events on its stream and its duration accumulated per
+ * kernel kind (adds a small overhead; off by default). */
+int pa_set_profiling(pa_ctx *ctx, int on);
+void pa_profile_reset(pa_ctx *ctx);
+/* Totals of kernel kind `kind` (0, 1, ...); returns PA_ERR_ARG past the
+ * last kind.  `items` counts the batch entries (spindowns or detectors)
+ * the launches processed. */
+int pa_profile_get(const pa_ctx *ctx, int kind, const char **name, double *total_ms,
+                   long long *launches, long long *items);
 
 #ifdef __cplusplus
 }

@@ -50,7 +50,35 @@ struct pa_ctx {
   int* h_ncand = nullptr;          // pinned
   std::string err;
   long long extra_launches = 0;
+  pa::Prof prof;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.;
 };
+
+namespace pa {
+const char* kernel_kind_name(int k) {
+  static const char* names[KK_COUNT] = {"prelude_mod", "prelude_sums", "resample_fft_fwd_a",
+                                        "resample_fft_fwd_b", "resample_fft_inv_a", "resample_fft_inv_b",
+                                        "spline_fwd", "spline_bwd", "splint", "spindown_pass_a",
+                                        "spindown_pass_b_fstat", "fstat_blockmean", "threshold"};
+  return (k >= 0 && k < KK_COUNT) ? names[k] : "";
+}
+}  // namespace pa
+
+// Accumulates the recorded per-launch events after the stream finished.
+static void prof_collect(pa_ctx* c) {
+  pa::Prof& p = c->prof;
+  for (int i = 0; i < p.n; i++) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.recs[i].a, p.recs[i].b) == cudaSuccess) {
+      p.total_ms[p.recs[i].kind] += ms;
+      p.launches[p.recs[i].kind] += 1;
+      p.items[p.recs[i].kind] += p.recs[i].items;
+    }
+  }
+  p.n = 0;
+  cudaGetLastError();
+}
 
 static int fail(pa_ctx* c, int code, const char* fmt, ...) {
   char buf[512];
@@ -274,6 +302,9 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   if ((rc = upload_data(c, det))) return rc;
   c->eng = c->fp64 ? pa::make_engine_f64(b) : pa::make_engine_f32(b, c->cfg.phase_mode);
   if (!c->eng) return fail(c, PA_ERR_NOMEM, "engine allocation failed");
+  c->eng->prof = &c->prof;
+  CK(cudaEventCreate(&c->ev0), "cudaEventCreate");
+  CK(cudaEventCreate(&c->ev1), "cudaEventCreate");
   return PA_OK;
 }
 
@@ -354,6 +385,13 @@ void pa_destroy(pa_ctx* c) {
   cudaSetDevice(c->dev);
   if (c->stream) cudaStreamSynchronize(c->stream);
   delete c->eng;
+  for (int i = 0; i < c->prof.cap; i++) {
+    cudaEventDestroy(c->prof.recs[i].a);
+    cudaEventDestroy(c->prof.recs[i].b);
+  }
+  delete[] c->prof.recs;
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
   for (void* p : c->allocs) cudaFree(p);
   if (c->h_cand) cudaFreeHost(c->h_cand);
   if (c->h_ncand) cudaFreeHost(c->h_ncand);
@@ -364,6 +402,44 @@ void pa_destroy(pa_ctx* c) {
 long long pa_kernel_launches(const pa_ctx* c) {
   if (!c) return 0;
   return (c->eng ? c->eng->launches() : 0) + c->extra_launches;
+}
+
+double pa_last_call_ms(const pa_ctx* c) { return c ? c->last_ms : 0.; }
+
+int pa_set_profiling(pa_ctx* c, int on) {
+  if (!c) return PA_ERR_ARG;
+  if (on && !c->prof.recs) {
+    CK(cudaSetDevice(c->dev), "cudaSetDevice");
+    const int cap = 1 << 16;
+    c->prof.recs = new pa::Prof::Rec[cap];
+    for (int i = 0; i < cap; i++) {
+      CK(cudaEventCreate(&c->prof.recs[i].a), "cudaEventCreate");
+      CK(cudaEventCreate(&c->prof.recs[i].b), "cudaEventCreate");
+      c->prof.cap = i + 1;
+    }
+  }
+  c->prof.on = on != 0;
+  return PA_OK;
+}
+
+void pa_profile_reset(pa_ctx* c) {
+  if (!c) return;
+  for (int k = 0; k < pa::KK_COUNT; k++) {
+    c->prof.total_ms[k] = 0.;
+    c->prof.launches[k] = 0;
+    c->prof.items[k] = 0;
+  }
+  c->prof.n = 0;
+}
+
+int pa_profile_get(const pa_ctx* c, int kind, const char** name, double* total_ms, long long* launches,
+                   long long* items) {
+  if (!c || kind < 0 || kind >= pa::KK_COUNT) return PA_ERR_ARG;
+  if (name) *name = pa::kernel_kind_name(kind);
+  if (total_ms) *total_ms = c->prof.total_ms[kind];
+  if (launches) *launches = c->prof.launches[kind];
+  if (items) *items = c->prof.items[kind];
+  return PA_OK;
 }
 
 }  // extern "C"
@@ -473,14 +549,22 @@ bool cand_less(const pa::DevCand& x, const pa::DevCand& y) {
 int run_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o, std::vector<pa::DevCand>* out) {
   CK(cudaSetDevice(c->dev), "cudaSetDevice");
   for (int attempt = 0; attempt < 3; attempt++) {
+    CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
     CK(cudaMemsetAsync(c->b.ncand, 0, sizeof(int), c->stream), "memset");
     for (size_t t = 0; t < hs.size(); t++) {
       if (!hs[t].inside || hs[t].nss == 0) continue;
       int rc = enqueue_sky(c, hs[t], o, (int)t, nullptr, 0);
       if (rc) return rc;
     }
+    CK(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
     CK(cudaMemcpyAsync(c->h_ncand, c->b.ncand, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "copy count");
     CK(cudaStreamSynchronize(c->stream), "search");
+    {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+      c->last_ms = ms;
+    }
+    if (c->prof.on) prof_collect(c);
     const int n = *c->h_ncand;
     if (n <= c->b.cand_cap) {
       if (n > 0) {
@@ -502,8 +586,11 @@ int run_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o, std::
     c->h_cand = nullptr;
     CK(cudaMallocHost((void**)&c->h_cand, sizeof(pa::DevCand) * (size_t)ncap), "cudaMallocHost");
     c->b.cand_cap = ncap;
+    const long long before = c->eng->launches();
     delete c->eng;
     c->eng = c->fp64 ? pa::make_engine_f64(c->b) : pa::make_engine_f32(c->b, c->cfg.phase_mode);
+    c->eng->prof = &c->prof;
+    c->extra_launches += before;
   }
   return fail(c, PA_ERR_CAPACITY, "device candidate buffer overflow");
 }

@@ -69,12 +69,17 @@ __global__ void __launch_bounds__(256)
                  k5 * sindel;
     a2 = (double)aa * (double)aa;
     b2 = (double)bb * (double)bb;
-    // shft, shftf, _tmp1 (jobcore.c:285-295), FP64
+    // shft, shftf, _tmp1 (jobcore.c:285-295), FP64 with the reference's
+    // rounding sequence (no FMA contraction): shftf[0] must be exactly 0, as
+    // shft1 comes from the same expression on the host; a contracted product
+    // would leave +-1 ulp there and push the spline abscissa 2(i - shftf)
+    // below 0, where splint returns 0 (auxi.c:89).
     const double* D = DetSSB + 3 * ((size_t)d * N + i);
-    const double shft = sky.nS[0] * D[0] + sky.nS[1] * D[1] + sky.nS[2] * D[2];
+    const double shft = __dadd_rn(__dadd_rn(__dmul_rn(sky.nS[0], D[0]), __dmul_rn(sky.nS[1], D[1])),
+                                  __dmul_rn(sky.nS[2], D[2]));
     shftf[(size_t)d * N + i] = shft - sky.shft1[d];
     const double di = (double)i;
-    const double tmp1 = di * di + (double)(2 * i) * shft;
+    const double tmp1 = __dadd_rn(__dmul_rn(di, di), __dmul_rn((double)(2 * i), shft));
     const size_t o = (size_t)d * N + i;
     if (PM == PM_FIXED) {
       // spindown phase s1(ss) tmp1 = s1_0 tmp1 + ss (M5 tmp1); both terms as
@@ -92,7 +97,7 @@ __global__ void __launch_bounds__(256)
       reinterpret_cast<double*>(ph0)[o] = tmp1;
     }
     // prelude phase het0 i + oms shft (jobcore.c:299), FP64
-    const double phase = sky.het0 * di + sky.oms * shft;
+    const double phase = __dadd_rn(__dmul_rn(sky.het0, di), __dmul_rn(sky.oms, shft));
     R sp, cp;
     if (sizeof(R) == 8) {
       double sd, cd;
@@ -256,7 +261,8 @@ template <typename R, int PM> struct SpinLoader {
       R sn, cs;
       if (sizeof(R) == 8) {
         const double t1 = reinterpret_cast<const double*>(ph0)[o];
-        const double ph = p->het1 * (double)n + p->s1 * t1;
+        // het1*i + s1*_tmp1 with the reference's rounding (jobcore.c:606)
+        const double ph = __dadd_rn(__dmul_rn(p->het1, (double)n), __dmul_rn(p->s1, t1));
         double sd, cd;
         sincos(ph, &sd, &cd);
         sn = (R)sd;
@@ -435,7 +441,7 @@ __global__ void __launch_bounds__(256)
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const int n = 2 * N;
-  const double x = 2 * (i - shftf[(size_t)d * N + i]);
+  const double x = __dmul_rn(2.0, __dsub_rn((double)i, shftf[(size_t)d * N + i]));
   const R is2 = (R)dc[d].inv_sig2;
   for (int arr = 0; arr < 2; ++arr) {
     const size_t q = (size_t)d * 2 + arr;
@@ -559,6 +565,22 @@ template <typename R, int PM> class EngineT : public Engine {
   Geom gf_, gi_, gm_;
   long long launches_ = 0;
 
+  // CUDA events around a launch when profiling is on
+  void pre(int kind, int items, cudaStream_t st) {
+    if (!prof || !prof->on) return;
+    if (prof->n == prof->cap) return;  // pool exhausted: stop recording
+    Prof::Rec& r = prof->recs[prof->n];
+    r.kind = kind;
+    r.items = items;
+    cudaEventRecord(r.a, st);
+  }
+  void post(cudaStream_t st) {
+    if (!prof || !prof->on) return;
+    if (prof->n == prof->cap) return;
+    cudaEventRecord(prof->recs[prof->n].b, st);
+    prof->n++;
+  }
+
   // opt-in above 48 KB of dynamic shared memory, once per kernel instance
   template <class K> static void smem_attr(K kernel, int bytes, bool& done) {
     if (!done) {
@@ -569,7 +591,7 @@ template <typename R, int PM> class EngineT : public Engine {
 
   template <int SIGN, class Loader, class Storer>
   cudaError_t fft(const Geom& g, const void* const* tw, const Loader& ld, const Storer& st, int batch,
-                  cudaStream_t stream) {
+                  cudaStream_t stream, int kind_a, int kind_b) {
     constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
     const T* t1 = (const T*)tw[0];
     const T* t2 = (const T*)tw[1];
@@ -584,8 +606,12 @@ template <typename R, int PM> class EngineT : public Engine {
     smem_attr(ka, (E + 1024) * (int)sizeof(T) + 128, doneA);
     smem_attr(kb, (E + 1024) * (int)sizeof(T), doneB);
     dim3 ga(g.L2 >> g.logC, batch), gb(g.L1 >> g.logRr, batch);
+    pre(kind_a, batch, stream);
     ka<<<ga, NT, smA, stream>>>(ld, g, t1, tlo, thi, yb);
+    post(stream);
+    pre(kind_b, batch, stream);
     kb<<<gb, NT, smB, stream>>>(st, g, t2, yb);
+    post(stream);
     launches_ += 2;
     return cudaGetLastError();
   }
@@ -603,31 +629,41 @@ template <typename R, int PM> class EngineT : public Engine {
   cudaError_t prelude(const SkyArgs& sky, cudaStream_t st) override {
     const int N = b_.N, nifo = b_.nifo;
     const int nbx = (N + 255) / 256;
+    pre(KK_PRELUDE_MOD, nifo, st);
     k_prelude_mod<R, PM><<<dim3(nbx, nifo), 256, 0, st>>>(
         b_.xDat, b_.DetSSB, (const R*)b_.cosmodf, (const R*)b_.sinmodf, b_.dc, sky, N, (T*)b_.xin,
         b_.shftf, b_.ph0, b_.ph1, b_.part);
+    post(st);
+    pre(KK_PRELUDE_SUMS, nifo, st);
     k_prelude_sums<<<1, 32, 0, st>>>(b_.part, nbx, nifo, b_.dc, b_.sums);
+    post(st);
     launches_ += 2;
     // forward FFT of the zero-padded series (length nfft)
     PlainLoader<R> pl{(const T*)b_.xin, N, N};
     CStore<R> cs1{(T*)b_.spec, b_.nfft, (R)1};
-    cudaError_t e = fft<-1>(gf_, b_.tw_fwd, pl, cs1, nifo, st);
+    cudaError_t e = fft<-1>(gf_, b_.tw_fwd, pl, cs1, nifo, st, KK_FFT_FWD_A, KK_FFT_FWD_B);
     if (e != cudaSuccess) return e;
     // spectrum remap + backward FFT (length Ninterp), scale interpftpad/Ninterp
     RemapLoader<R> rl{(const T*)b_.spec, b_.nfft, b_.nfft / 2 + 1, b_.Ninterp - b_.nfft};
     CStore<R> cs2{(T*)b_.yint, b_.Ninterp, (R)(2.0 / b_.Ninterp)};
-    e = fft<+1>(gi_, b_.tw_inv, rl, cs2, nifo, st);
+    e = fft<+1>(gi_, b_.tw_inv, rl, cs2, nifo, st, KK_FFT_INV_A, KK_FFT_INV_B);
     if (e != cudaSuccess) return e;
     // spline through the first 2N points of each resampled array
     const int n = 2 * N;
     const int nch = (n + kSplineChunk - 1) / kSplineChunk;
     const int nthr = nch * 2 * nifo;
+    pre(KK_SPLINE_FWD, nifo, st);
     k_spline_fwd<R><<<(nthr + 127) / 128, 128, 0, st>>>((const T*)b_.yint, b_.Ninterp, (double2*)b_.u,
                                                         n, nch, 2 * nifo, b_.spline_invp);
+    post(st);
+    pre(KK_SPLINE_BWD, nifo, st);
     k_spline_bwd<R><<<(nthr + 127) / 128, 128, 0, st>>>((const double2*)b_.u, (T*)b_.y2, n, nch,
                                                         2 * nifo, b_.spline_p);
+    post(st);
+    pre(KK_SPLINT, nifo, st);
     k_splint<R><<<dim3(nbx, nifo), 256, 0, st>>>((const T*)b_.yint, b_.Ninterp, (const T*)b_.y2,
                                                  b_.shftf, b_.dc, N, (T*)b_.xm);
+    post(st);
     launches_ += 3;
     return cudaGetLastError();
   }
@@ -647,16 +683,20 @@ template <typename R, int PM> class EngineT : public Engine {
     sl.M5 = sky.M5;
     sl.s1_0 = sky.s1_0;
     FstatStore<R> fs{(R*)b_.F, b_.sums, b_.nmin, b_.nmax, b_.bins};
-    cudaError_t e = fft<-1>(gm_, b_.tw_main, sl, fs, nb, st);
+    cudaError_t e = fft<-1>(gm_, b_.tw_main, sl, fs, nb, st, KK_SPIN_A, KK_SPIN_B);
     if (e != cudaSuccess) return e;
     if (b_.nblk > 0 && !white) {
+      pre(KK_BLOCKMEAN, nb, st);
       k_blockmean<R><<<dim3(b_.nblk, nb), 256, 0, st>>>((const R*)b_.F, b_.bins, b_.nblk, (R*)b_.mu);
+      post(st);
       launches_ += 1;
     }
     const int nchunk = (b_.bins + 4095) / 4096;
+    pre(KK_THRESHOLD, nb, st);
     k_threshold<R><<<dim3(nchunk, nb), 256, 0, st>>>((const R*)b_.F, b_.bins, b_.nblk, (const R*)b_.mu,
                                                      white, (R)trl, b_.nmin, ss0, sky.task, b_.cand,
                                                      b_.ncand, b_.cand_cap, (R*)Fdbg);
+    post(st);
     launches_ += 1;
     return cudaGetLastError();
   }

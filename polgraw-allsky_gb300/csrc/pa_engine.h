@@ -70,8 +70,30 @@ struct Buffers {
   const void* tw_main[4];           // nfftf forward
 };
 
+// Kernel kinds for the optional per-launch CUDA-event profile.
+enum KernelKind {
+  KK_PRELUDE_MOD = 0, KK_PRELUDE_SUMS, KK_FFT_FWD_A, KK_FFT_FWD_B, KK_FFT_INV_A, KK_FFT_INV_B,
+  KK_SPLINE_FWD, KK_SPLINE_BWD, KK_SPLINT, KK_SPIN_A, KK_SPIN_B, KK_BLOCKMEAN, KK_THRESHOLD, KK_COUNT
+};
+const char* kernel_kind_name(int k);
+
+// Event-bracketed launches recorded while profiling is on.
+struct Prof {
+  bool on = false;
+  struct Rec {
+    int kind, items;
+    cudaEvent_t a, b;
+  };
+  Rec* recs = nullptr;
+  int n = 0, cap = 0;
+  double total_ms[KK_COUNT] = {0};
+  long long launches[KK_COUNT] = {0};
+  long long items[KK_COUNT] = {0};
+};
+
 class Engine {
  public:
+  Prof* prof = nullptr;  // owned by the context
   virtual ~Engine() {}
   // Enqueues the per-sky prelude (jobcore.c:270-393) on `st`.
   virtual cudaError_t prelude(const SkyArgs& sky, cudaStream_t st) = 0;

@@ -26,6 +26,7 @@ PHASE_NAMES = {"f64": PA_PHASE_F64, "fixed": PA_PHASE_FIXED, "ff": PA_PHASE_FF}
 EXPORTS = [
     "pa_version", "pa_device_count", "pa_create", "pa_set_data", "pa_destroy", "pa_last_error",
     "pa_job_core", "pa_search_batch", "pa_debug_prelude", "pa_debug_fstat", "pa_kernel_launches",
+    "pa_last_call_ms", "pa_set_profiling", "pa_profile_reset", "pa_profile_get",
     "pa_host_create", "pa_host_setup", "pa_host_search", "pa_host_main", "pa_host_destroy",
     "pa_host_settings", "pa_host_detectors", "pa_host_range", "pa_host_core_opts",
     "pa_host_config", "pa_host_detector_name",
@@ -99,6 +100,13 @@ def load(path: str | None = None) -> C.CDLL:
     lib.pa_debug_fstat.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, P(Opts), P(C.c_double)]
     lib.pa_kernel_launches.restype = C.c_longlong
     lib.pa_kernel_launches.argtypes = [C.c_void_p]
+    lib.pa_last_call_ms.restype = C.c_double
+    lib.pa_last_call_ms.argtypes = [C.c_void_p]
+    lib.pa_set_profiling.argtypes = [C.c_void_p, C.c_int]
+    lib.pa_profile_reset.argtypes = [C.c_void_p]
+    lib.pa_profile_reset.restype = None
+    lib.pa_profile_get.argtypes = [C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_longlong),
+                                   P(C.c_longlong)]
     lib.pa_host_create.restype = C.c_void_p
     lib.pa_host_create.argtypes = [C.c_int, P(C.c_char_p), P(C.c_int)]
     lib.pa_host_setup.argtypes = [C.c_void_p]
@@ -282,6 +290,32 @@ class Context:
 
     def launches(self) -> int:
         return int(self.lib.pa_kernel_launches(self.ctx))
+
+    def last_call_ms(self) -> float:
+        return float(self.lib.pa_last_call_ms(self.ctx))
+
+    def set_profiling(self, on: bool):
+        rc = self.lib.pa_set_profiling(self.ctx, 1 if on else 0)
+        if rc != PA_OK:
+            raise SearchError("pa_set_profiling failed: %s" % self.error())
+
+    def profile_reset(self):
+        self.lib.pa_profile_reset(self.ctx)
+
+    def profile(self) -> dict:
+        """{kernel name: (total_ms, launches, items)}"""
+        out = {}
+        k = 0
+        while True:
+            name = C.c_char_p()
+            ms = C.c_double()
+            nl = C.c_longlong()
+            it = C.c_longlong()
+            if self.lib.pa_profile_get(self.ctx, k, C.byref(name), C.byref(ms), C.byref(nl), C.byref(it)) != PA_OK:
+                break
+            out[name.value.decode()] = (ms.value, nl.value, it.value)
+            k += 1
+        return out
 
     def close(self):
         if self.ctx:
