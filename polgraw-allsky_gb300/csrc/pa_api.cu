@@ -41,7 +41,9 @@ struct pa_ctx {
   pa::DetConst dc[pa::kMaxDet];
   double det0[pa::kMaxDet][3];  // DetSSB of sample 0 (shft1)
   int dev = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // spindown loop, copies
+  cudaStream_t stream_pre = nullptr;  // per-sky preludes
+  cudaEvent_t ev_pre[2] = {nullptr, nullptr}, ev_spin[2] = {nullptr, nullptr};
   pa::Buffers b;
   std::vector<void*> allocs;
   Twiddles tw_fwd, tw_inv, tw_main;
@@ -218,6 +220,11 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   const int N = s.N, nifo = c->nifo;
   CK(cudaSetDevice(c->dev), "cudaSetDevice");
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  CK(cudaStreamCreateWithFlags(&c->stream_pre, cudaStreamNonBlocking), "cudaStreamCreate");
+  for (int k = 0; k < 2; k++) {
+    CK(cudaEventCreateWithFlags(&c->ev_pre[k], cudaEventDisableTiming), "cudaEventCreate");
+    CK(cudaEventCreateWithFlags(&c->ev_spin[k], cudaEventDisableTiming), "cudaEventCreate");
+  }
   pa::Buffers& b = c->b;
   memset(&b, 0, sizeof(b));
   b.N = N;
@@ -258,13 +265,18 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   ALLOC(b.u, sizeof(double) * 2 * nifo * 2 * (size_t)(2 * N));
   ALLOC(b.y2, cs * nifo * 2 * (size_t)(2 * N));
   ALLOC(b.shftf, sizeof(double) * nifo * (size_t)N);
-  ALLOC(b.ph0, 8 * nifo * (size_t)N);
-  ALLOC(b.ph1, 8 * nifo * (size_t)N);
-  ALLOC(b.xm, cs * nifo * 2 * (size_t)N);
+  for (int k = 0; k < 2; k++) {
+    ALLOC(b.ph0[k], 8 * nifo * (size_t)N);
+    ALLOC(b.ph1[k], 8 * nifo * (size_t)N);
+    ALLOC(b.xm[k], cs * nifo * 2 * (size_t)N);
+    ALLOC(b.sums[k], sizeof(double) * 8);
+    ALLOC(b.sums_r[k], sizeof(double) * 4);
+  }
   ALLOC(b.part, sizeof(double) * 2 * nifo * (size_t)((N + 255) / 256));
-  ALLOC(b.sums, sizeof(double) * 8);
-  const size_t ybytes = std::max((size_t)sb * 2 * s.nfftf, (size_t)nifo * 2 * s.Ninterp) * cs;
-  ALLOC(b.ybuf, ybytes);
+  ALLOC(b.ybuf_pre, cs * nifo * 2 * (size_t)s.Ninterp);
+  ALLOC(b.counter, sizeof(unsigned int) * 4);
+  CK(cudaMemset(b.counter, 0, sizeof(unsigned int) * 4), "cudaMemset");
+  ALLOC(b.ybuf, (size_t)sb * 2 * s.nfftf * cs);
   ALLOC(b.F, rs * (size_t)sb * b.bins);
   ALLOC(b.mu, rs * (size_t)sb * (b.nblk > 0 ? b.nblk : 1));
   b.cand_cap = 1 << 18;
@@ -384,6 +396,7 @@ void pa_destroy(pa_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->dev);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->stream_pre) cudaStreamSynchronize(c->stream_pre);
   delete c->eng;
   for (int i = 0; i < c->prof.cap; i++) {
     cudaEventDestroy(c->prof.recs[i].a);
@@ -396,6 +409,11 @@ void pa_destroy(pa_ctx* c) {
   if (c->h_cand) cudaFreeHost(c->h_cand);
   if (c->h_ncand) cudaFreeHost(c->h_ncand);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->stream_pre) cudaStreamDestroy(c->stream_pre);
+  for (int k = 0; k < 2; k++) {
+    if (c->ev_pre[k]) cudaEventDestroy(c->ev_pre[k]);
+    if (c->ev_spin[k]) cudaEventDestroy(c->ev_spin[k]);
+  }
   delete c;
 }
 
@@ -519,21 +537,40 @@ void sky_setup(const pa_ctx* c, int pm, int mm, int nn, const pa_opts* o, int ss
   a.task = 0;
 }
 
-int enqueue_sky(pa_ctx* c, const SkyHost& h, const pa_opts* o, int task, void* Fdbg, int Fss) {
+// Kernel arguments of a sky point for this context's engine.
+pa::SkyArgs sky_args(const pa_ctx* c, const SkyHost& h, int task) {
   pa::SkyArgs a = h.args;
   a.task = task;
-  cudaError_t e = c->eng->prelude(a, c->stream);
+  if (!c->fp64 && c->cfg.phase_mode == PA_PHASE_FIXED) {
+    // the fixed-point phase terms are formed in turns
+    a.s1_0 = a.s1_0 / (2. * M_PI);
+    a.M5 = a.M5 / (2. * M_PI);
+  }
+  return a;
+}
+
+// Enqueues one sky point: its prelude on the prelude stream into slot
+// task % 2 (after the spindowns that last read that slot), and its spindown
+// batches on the main stream (after the prelude).
+int enqueue_sky(pa_ctx* c, const SkyHost& h, const pa_opts* o, int task, void* Fdbg, int Fss) {
+  const pa::SkyArgs a = sky_args(c, h, task);
+  const int slot = task & 1;
+  CK(cudaStreamWaitEvent(c->stream_pre, c->ev_spin[slot], 0), "cudaStreamWaitEvent");
+  cudaError_t e = c->eng->prelude(a, slot, c->stream_pre);
   if (e != cudaSuccess) return cuda_fail(c, e, "prelude launch");
+  CK(cudaEventRecord(c->ev_pre[slot], c->stream_pre), "cudaEventRecord");
+  CK(cudaStreamWaitEvent(c->stream, c->ev_pre[slot], 0), "cudaStreamWaitEvent");
   if (Fdbg) {
-    e = c->eng->spindowns(a, Fss, 1, o->trl, o->white_flag, o->s0_flag, c->stream, Fdbg);
+    e = c->eng->spindowns(a, slot, Fss, 1, o->trl, o->white_flag, o->s0_flag, c->stream, Fdbg);
     if (e != cudaSuccess) return cuda_fail(c, e, "spindown launch");
-    return PA_OK;
+  } else {
+    for (int ss = h.smin; ss <= h.smax; ss += c->b.sbatch) {
+      const int nb = std::min(c->b.sbatch, h.smax - ss + 1);
+      e = c->eng->spindowns(a, slot, ss, nb, o->trl, o->white_flag, o->s0_flag, c->stream, nullptr);
+      if (e != cudaSuccess) return cuda_fail(c, e, "spindown launch");
+    }
   }
-  for (int ss = h.smin; ss <= h.smax; ss += c->b.sbatch) {
-    const int nb = std::min(c->b.sbatch, h.smax - ss + 1);
-    e = c->eng->spindowns(a, ss, nb, o->trl, o->white_flag, o->s0_flag, c->stream, nullptr);
-    if (e != cudaSuccess) return cuda_fail(c, e, "spindown launch");
-  }
+  CK(cudaEventRecord(c->ev_spin[slot], c->stream), "cudaEventRecord");
   return PA_OK;
 }
 
@@ -551,11 +588,16 @@ int run_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o, std::
   for (int attempt = 0; attempt < 3; attempt++) {
     CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
     CK(cudaMemsetAsync(c->b.ncand, 0, sizeof(int), c->stream), "memset");
+    // the prelude stream starts after ev0 so the timing covers its work
+    CK(cudaStreamWaitEvent(c->stream_pre, c->ev0, 0), "cudaStreamWaitEvent");
+    int nq = 0;
     for (size_t t = 0; t < hs.size(); t++) {
       if (!hs[t].inside || hs[t].nss == 0) continue;
       int rc = enqueue_sky(c, hs[t], o, (int)t, nullptr, 0);
       if (rc) return rc;
+      nq++;
     }
+    (void)nq;
     CK(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
     CK(cudaMemcpyAsync(c->h_ncand, c->b.ncand, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "copy count");
     CK(cudaStreamSynchronize(c->stream), "search");
@@ -683,14 +725,15 @@ int pa_debug_prelude(pa_ctx* c, int pm, int mm, int nn, double* xa, double* xb, 
   SkyHost h;
   sky_setup(c, pm, mm, nn, &o, 0, 0, &h);
   if (!h.inside) return fail(c, PA_ERR_ARG, "sky point outside the grid disk");
-  cudaError_t e = c->eng->prelude(h.args, c->stream);
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  cudaError_t e = c->eng->prelude(sky_args(c, h, 0), 0, c->stream_pre);
   if (e != cudaSuccess) return cuda_fail(c, e, "prelude");
   const size_t n = (size_t)c->nifo * 2 * c->sett.N;
   std::vector<char> buf(n * 2 * c->rsz);
   double sums[4];
-  CK(cudaMemcpyAsync(buf.data(), c->b.xm, buf.size(), cudaMemcpyDeviceToHost, c->stream), "copy");
-  CK(cudaMemcpyAsync(sums, c->b.sums, sizeof(sums), cudaMemcpyDeviceToHost, c->stream), "copy");
-  CK(cudaStreamSynchronize(c->stream), "prelude");
+  CK(cudaMemcpyAsync(buf.data(), c->b.xm[0], buf.size(), cudaMemcpyDeviceToHost, c->stream_pre), "copy");
+  CK(cudaMemcpyAsync(sums, c->b.sums[0], sizeof(sums), cudaMemcpyDeviceToHost, c->stream_pre), "copy");
+  CK(cudaStreamSynchronize(c->stream_pre), "prelude");
   const int N = c->sett.N;
   for (int d = 0; d < c->nifo; d++)
     for (int arr = 0; arr < 2; arr++) {

@@ -35,8 +35,50 @@ constexpr float kTwoPiF_B = 1.9353071693331003e-3f;
 constexpr float kTwoPiF_C = 1.0253131677018246e-11f;
 constexpr float kInvTwoPiF = 0.15915494309189533577f;
 
+// x mod 1 as a 64-bit fixed-point fraction (t / 2^64), computed exactly
+// from the bits of x with integer operations only: x = m 2^(e-1075) with the
+// 53-bit integer significand m, so x 2^64 mod 2^64 = m << (e - 1011) (or
+// >> for negative shifts), negated for x < 0.
+__device__ __forceinline__ uint64_t turns_fixed(double x) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  if (e == 0) return 0ull;  // zero or subnormal: |x| < 2^-1022
+  const unsigned long long m = (bits & 0xfffffffffffffull) | 0x10000000000000ull;
+  const int sh = e - 1011;
+  unsigned long long t;
+  if (sh >= 64) t = 0ull;
+  else if (sh >= 0) t = m << sh;
+  else if (sh > -64) t = m >> (-sh);
+  else t = 0ull;
+  return (bits >> 63) ? (0ull - t) : t;
+}
+
 // ------------------------------------------------------------------
 // prelude: modvir + time shift + prelude phase modulation
+
+// Sum of two values over a 256-thread block in a fixed order (xor tree in
+// each warp, then warps in index order); the result is valid in every thread.
+__device__ __forceinline__ void block_sum2(double& a, double& b, double (*red)[8]) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, off);
+    b += __shfl_xor_sync(0xffffffffu, b, off);
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][w] = a;
+    red[1][w] = b;
+  }
+  __syncthreads();
+  double sa = 0., sb = 0.;
+  for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+    sa += red[0][k];
+    sb += red[1][k];
+  }
+  __syncthreads();
+  a = sa;
+  b = sb;
+}
 
 template <typename R, int PM>
 __global__ void __launch_bounds__(256)
@@ -44,11 +86,12 @@ __global__ void __launch_bounds__(256)
                   const R* __restrict__ cosmodf, const R* __restrict__ sinmodf,
                   const DetConst* __restrict__ dc, const SkyArgs sky, int N,
                   typename CT<R>::T* __restrict__ xin, double* __restrict__ shftf, void* ph0,
-                  void* ph1, double* __restrict__ part) {
+                  void* ph1, double* __restrict__ part, double* __restrict__ sums, R* __restrict__ sums_r,
+                  unsigned int* __restrict__ counter) {
   typedef typename CT<R>::T T;
   const int d = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double a2 = 0., b2 = 0.;
+  R a2r = 0, b2r = 0;
   if (i < N) {
     const DetConst& k = dc[d];
     // modvir, settings.c:303-322
@@ -67,8 +110,8 @@ __global__ void __launch_bounds__(256)
                  k0 * two_m + k4 * c2d;
     const R bb = k5 * sindel * c2s + k6 * sindel * (R)2 * cs + k7 * cosdel * c + k8 * cosdel * s -
                  k5 * sindel;
-    a2 = (double)aa * (double)aa;
-    b2 = (double)bb * (double)bb;
+    a2r = aa * aa;
+    b2r = bb * bb;
     // shft, shftf, _tmp1 (jobcore.c:285-295), FP64 with the reference's
     // rounding sequence (no FMA contraction): shftf[0] must be exactly 0, as
     // shft1 comes from the same expression on the host; a contracted product
@@ -83,13 +126,10 @@ __global__ void __launch_bounds__(256)
     const size_t o = (size_t)d * N + i;
     if (PM == PM_FIXED) {
       // spindown phase s1(ss) tmp1 = s1_0 tmp1 + ss (M5 tmp1); both terms as
-      // 64-bit fixed-point fractions of a turn
-      double fa = sky.s1_0 * tmp1 * kInvTwoPi;
-      fa -= floor(fa);
-      double fb = sky.M5 * tmp1 * kInvTwoPi;
-      fb -= floor(fb);
-      reinterpret_cast<uint64_t*>(ph0)[o] = (uint64_t)__double2ull_rn(fa * 18446744073709551616.0);
-      reinterpret_cast<uint64_t*>(ph1)[o] = (uint64_t)__double2ull_rn(fb * 18446744073709551616.0);
+      // 64-bit fixed-point fractions of a turn (sky.s1_0 and sky.M5 hold the
+      // values divided by 2 pi for this mode)
+      reinterpret_cast<uint64_t*>(ph0)[o] = turns_fixed(sky.s1_0 * tmp1);
+      reinterpret_cast<uint64_t*>(ph1)[o] = turns_fixed(sky.M5 * tmp1);
     } else if (PM == PM_FF) {
       const float hi = (float)tmp1;
       reinterpret_cast<float2*>(ph0)[o] = make_float2(hi, (float)(tmp1 - (double)hi));
@@ -105,11 +145,10 @@ __global__ void __launch_bounds__(256)
       sp = (R)sd;
       cp = (R)cd;
     } else {
-      const double kk = rint(phase * kInvTwoPi);
-      double r = fma(-kk, kTwoPiHi, phase);
-      r = fma(-kk, kTwoPiLo, r);
+      // reduce in turns: exact fraction from the FP64 value, then FP32
+      const uint64_t t = turns_fixed(phase * kInvTwoPi);
       float sf, cf;
-      sincosf((float)r, &sf, &cf);
+      sincospif((float)(int)(t >> 32) * 4.656612873077393e-10f, &sf, &cf);
       sp = (R)sf;
       cp = (R)cf;
     }
@@ -119,60 +158,58 @@ __global__ void __launch_bounds__(256)
     xin[((size_t)d * 2 + 0) * N + i] = mk(xa * cp, -xa * sp);
     xin[((size_t)d * 2 + 1) * N + i] = mk(xb * cp, -xb * sp);
   }
-  // deterministic block reduction of a^2, b^2
-  __shared__ double red[2][8];
+  // deterministic block reduction of a^2, b^2: xor tree of each warp in the
+  // working precision, warps summed in FP64 in index order
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    a2 += __shfl_xor_sync(0xffffffffu, a2, off);
-    b2 += __shfl_xor_sync(0xffffffffu, b2, off);
+    a2r += __shfl_xor_sync(0xffffffffu, a2r, off);
+    b2r += __shfl_xor_sync(0xffffffffu, b2r, off);
   }
-  const int w = threadIdx.x >> 5;
+  __shared__ double red[2][8];
+  __shared__ bool last;
   if ((threadIdx.x & 31) == 0) {
-    red[0][w] = a2;
-    red[1][w] = b2;
+    red[0][threadIdx.x >> 5] = (double)a2r;
+    red[1][threadIdx.x >> 5] = (double)b2r;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double sa = 0., sb = 0.;
+  double a2 = 0., b2 = 0.;
+  if (threadIdx.x == 0)
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-      sa += red[0][k];
-      sb += red[1][k];
+      a2 += red[0][k];
+      b2 += red[1][k];
     }
-    part[((size_t)d * gridDim.x + blockIdx.x) * 2 + 0] = sa;
-    part[((size_t)d * gridDim.x + blockIdx.x) * 2 + 1] = sb;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    part[((size_t)d * gridDim.x + blockIdx.x) * 2 + 0] = a2;
+    part[((size_t)d * gridDim.x + blockIdx.x) * 2 + 1] = b2;
+    __threadfence();
+    const unsigned int done = atomicAdd(counter, 1u);
+    last = done == gridDim.x * gridDim.y - 1;
   }
-}
-
-// aa = sum_n (sum_i a^2)/sig2_n, bb likewise (jobcore.c:375-393)
-static __global__ void k_prelude_sums(const double* __restrict__ part, int nblocks, int nifo,
-                               const DetConst* __restrict__ dc, double* __restrict__ sums) {
-  __shared__ double red[2][32];
+  __syncthreads();
+  if (!last) return;
+  // the last CTA to finish: aa = sum_n (sum_i a^2)/sig2_n in detector order
+  // (jobcore.c:375-393), partials summed in a fixed order
   double aa = 0., bb = 0.;
-  for (int d = 0; d < nifo; ++d) {
+  for (int dd = 0; dd < (int)gridDim.y; ++dd) {
     double sa = 0., sb = 0.;
-    for (int b = threadIdx.x; b < nblocks; b += 32) {
-      sa += part[((size_t)d * nblocks + b) * 2 + 0];
-      sb += part[((size_t)d * nblocks + b) * 2 + 1];
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+      sa += __ldcg(&part[((size_t)dd * gridDim.x + k) * 2 + 0]);
+      sb += __ldcg(&part[((size_t)dd * gridDim.x + k) * 2 + 1]);
     }
-    red[0][threadIdx.x] = sa;
-    red[1][threadIdx.x] = sb;
-    __syncwarp();
-    if (threadIdx.x == 0) {
-      double ta = 0., tb = 0.;
-      for (int k = 0; k < 32; ++k) {
-        ta += red[0][k];
-        tb += red[1][k];
-      }
-      aa += ta / dc[d].sig2;
-      bb += tb / dc[d].sig2;
-    }
-    __syncwarp();
+    __syncthreads();
+    block_sum2(sa, sb, red);
+    aa += sa / dc[dd].sig2;
+    bb += sb / dc[dd].sig2;
   }
   if (threadIdx.x == 0) {
     sums[0] = aa;
     sums[1] = bb;
     sums[2] = 1.0 / aa;
     sums[3] = 1.0 / bb;
+    sums_r[0] = (R)(1.0 / aa);
+    sums_r[1] = (R)(1.0 / bb);
+    *counter = 0u;
   }
 }
 
@@ -281,8 +318,10 @@ template <typename R, int PM> struct SpinLoader {
         const uint64_t A = reinterpret_cast<const uint64_t*>(ph0)[o];
         const uint64_t B = reinterpret_cast<const uint64_t*>(ph1)[o];
         const uint64_t t = A + (uint64_t)p->ss * B + ibase;
-        // fraction of a turn as a signed value in [-1/2, 1/2) -> pi * x
-        const float x = (float)(long long)t * 1.0842021724855044e-19f;  // 2^-63
+        // top 32 bits as a signed fraction of half a turn: angle = pi * x,
+        // x in [-1, 1) (resolution 2^-31 half-turns = 1.5e-9 rad); the
+        // 32-bit conversion stays off the FP64 pipe
+        const float x = (float)(int)(t >> 32) * 4.656612873077393e-10f;  // 2^-31
         float sf, cf;
         sincospif(x, &sf, &cf);
         sn = (R)sf;
@@ -331,16 +370,11 @@ template <typename R> struct CStore {
   T* out;   // [batch][2][ldo]
   int ldo;
   R scale;
-  __device__ __forceinline__ void store(int batch, int t, const T* s, const Geom& g) const {
-    constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
-    const int rmask = g.Rr - 1;
-    for (int w = threadIdx.x; w < E; w += NT) {
-      const int r = w & rmask, rest = w >> g.logRr;
-      const int arr = rest & 1, k2 = rest >> 1;
-      const int k = (t << g.logRr) + r + (k2 << g.logL1);
-      const T v = s[(k2 << (g.logRr + 1)) + arr * g.Rr + r];
-      out[((size_t)batch * 2 + arr) * ldo + k] = mk(v.x * scale, v.y * scale);
-    }
+  __device__ __forceinline__ void begin(int, int) const {}
+  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, const Geom& g) const {
+    const size_t k = (size_t)k1 + ((size_t)k2 << g.logL1);
+    out[((size_t)batch * 2 + 0) * ldo + k] = mk(a.x * scale, a.y * scale);
+    out[((size_t)batch * 2 + 1) * ldo + k] = mk(b.x * scale, b.y * scale);
   }
 };
 
@@ -348,21 +382,14 @@ template <typename R> struct CStore {
 template <typename R> struct FstatStore {
   typedef typename CT<R>::T T;
   R* F;             // [batch][bins]
-  const double* sums;
+  const R* inv;     // 1/aa, 1/bb in the working precision
   int nmin, nmax, bins;
-  __device__ __forceinline__ void store(int batch, int t, const T* s, const Geom& g) const {
-    constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
-    const R ia = (R)sums[2], ib = (R)sums[3];
-    const int rmask = g.Rr - 1;
-    R* Fb = F + (size_t)batch * bins - nmin;
-    for (int w = threadIdx.x; w < (E >> 1); w += NT) {
-      const int r = w & rmask, k2 = w >> g.logRr;
-      const int k = (t << g.logRr) + r + (k2 << g.logL1);
-      if (k >= nmin && k < nmax) {
-        const T xa = s[(k2 << (g.logRr + 1)) + r];
-        const T xb = s[(k2 << (g.logRr + 1)) + g.Rr + r];
-        Fb[k] = (xa.x * xa.x + xa.y * xa.y) * ia + (xb.x * xb.x + xb.y * xb.y) * ib;
-      }
+  __device__ __forceinline__ void begin(int, int) const {}
+  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, const Geom& g) const {
+    const int k = k1 + (k2 << g.logL1);
+    if (k >= nmin && k < nmax) {
+      const R ia = __ldg(&inv[0]), ib = __ldg(&inv[1]);
+      F[(size_t)batch * bins + (k - nmin)] = (a.x * a.x + a.y * a.y) * ia + (b.x * b.x + b.y * b.y) * ib;
     }
   }
 };
@@ -376,58 +403,95 @@ template <typename R> struct FstatStore {
 // from the exact boundary values u_0 = 0, y2_{n-1} = 0.
 constexpr int kSplineChunk = 64;
 constexpr int kSplineWarm = 32;
+constexpr int kSplineChunks = 64;                          // recurrence threads per CTA
+constexpr int kSplineThreads = 256;                        // threads for staging loads/stores
+constexpr int kSplineSeg = kSplineChunk * kSplineChunks;   // elements per CTA
 
+// Forward sweep.  A CTA owns one segment of kSplineSeg elements of one
+// array; it stages y[seg - warm - 1, seg_end + 1) in shared memory with
+// coalesced loads (as FP64), every thread runs its chunk's recurrence from
+// shared memory, and the u values leave through shared memory again so the
+// global stores are coalesced.
 template <typename R>
-__global__ void __launch_bounds__(128)
-    k_spline_fwd(const typename CT<R>::T* __restrict__ y, int ldy, double2* __restrict__ u, int n,
-                 int nchunks, int narr, const double* __restrict__ invp) {
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= nchunks * narr) return;
-  const int q = gid / nchunks, c = gid - q * nchunks;
-  const typename CT<R>::T* yq = y + (size_t)q * ldy;
+__global__ void __launch_bounds__(kSplineThreads)
+    k_spline_fwd(const typename CT<R>::T* __restrict__ y, int ldy, double2* __restrict__ u, int n, int nseg,
+                 const double* __restrict__ invp) {
+  typedef typename CT<R>::T T;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  double2* us = reinterpret_cast<double2*>(sm_raw);           // kSplineSeg
+  T* ys = reinterpret_cast<T*>(us + kSplineSeg);              // kSplineSeg + kSplineWarm + 2
+  const int q = blockIdx.x / nseg, sg = blockIdx.x - q * nseg;
+  const T* yq = y + (size_t)q * ldy;
   double2* uq = u + (size_t)q * n;
-  const int lo = c * kSplineChunk;
-  const int hi = min(lo + kSplineChunk, n - 1);
-  if (c == 0) uq[0] = make_double2(0., 0.);
-  int i = max(1, lo - kSplineWarm);
-  double ux = 0., uy = 0.;
-  double pxr = (double)yq[i - 1].x, pyr = (double)yq[i - 1].y;
-  double cxr = (double)yq[i].x, cyr = (double)yq[i].y;
-  for (; i < hi; ++i) {
-    const double nxr = (double)yq[i + 1].x, nyr = (double)yq[i + 1].y;
-    const double dx = pxr - 2. * cxr + nxr, dy = pyr - 2. * cyr + nyr;
-    const double ip = invp[i < 64 ? i : 63];
-    ux = (-.5 * ux + 3. * dx) * ip;
-    uy = (-.5 * uy + 3. * dy) * ip;
-    if (i >= lo) uq[i] = make_double2(ux, uy);
-    pxr = cxr;
-    pyr = cyr;
-    cxr = nxr;
-    cyr = nyr;
+  const int seg0 = sg * kSplineSeg;
+  const int y0 = seg0 - kSplineWarm - 1;                       // first staged index
+  const int ny = kSplineSeg + kSplineWarm + 2;
+  for (int k = threadIdx.x; k < ny; k += kSplineThreads) {
+    const int i = y0 + k;
+    ys[k] = (i >= 0 && i < n) ? yq[i] : mk((R)0, (R)0);
   }
+  __syncthreads();
+  if (threadIdx.x < kSplineChunks) {
+    const int lo = seg0 + threadIdx.x * kSplineChunk;
+    const int hi = min(lo + kSplineChunk, n - 1);
+    // u_i = (-u_{i-1}/2 + 3 d_i) invp_i = al_i u_{i-1} + be_i d_i in FP64;
+    // the second difference d_i of the working-precision data is formed in
+    // that precision (its rounding is below the data's own)
+    int i = max(1, lo - kSplineWarm);
+    double ux = 0., uy = 0.;
+    T p = ys[i - 1 - y0], cc = ys[i - y0];
+    for (; i < hi; ++i) {
+      const T nn = ys[i + 1 - y0];
+      const R dx = p.x - (R)2 * cc.x + nn.x, dy = p.y - (R)2 * cc.y + nn.y;
+      const int ti = i < 64 ? i : 63;
+      const double al = -.5 * invp[ti], be = 3. * invp[ti];
+      ux = fma(al, ux, be * (double)dx);
+      uy = fma(al, uy, be * (double)dy);
+      if (i >= lo) us[i - seg0] = make_double2(ux, uy);
+      p = cc;
+      cc = nn;
+    }
+    if (lo == 0) us[0] = make_double2(0., 0.);
+  }
+  __syncthreads();
+  const int cnt = min(kSplineSeg, n - 1 - seg0);
+  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) uq[seg0 + k] = us[k];
 }
 
+// Back substitution, same staging: u[seg0, seg_end + warm) in shared memory,
+// y2 of the segment written back through shared memory.
 template <typename R>
-__global__ void __launch_bounds__(128)
-    k_spline_bwd(const double2* __restrict__ u, typename CT<R>::T* __restrict__ y2, int n,
-                 int nchunks, int narr, const double* __restrict__ ptab) {
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= nchunks * narr) return;
-  const int q = gid / nchunks, c = gid - q * nchunks;
+__global__ void __launch_bounds__(kSplineThreads)
+    k_spline_bwd(const double2* __restrict__ u, typename CT<R>::T* __restrict__ y2, int n, int nseg,
+                 const double* __restrict__ ptab) {
+  typedef typename CT<R>::T T;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  double2* us = reinterpret_cast<double2*>(sm_raw);           // kSplineSeg + kSplineWarm
+  T* ys = reinterpret_cast<T*>(us + kSplineSeg + kSplineWarm);  // kSplineSeg
+  const int q = blockIdx.x / nseg, sg = blockIdx.x - q * nseg;
   const double2* uq = u + (size_t)q * n;
-  typename CT<R>::T* yq = y2 + (size_t)q * n;
-  const int lo = c * kSplineChunk;
+  T* yq = y2 + (size_t)q * n;
+  const int seg0 = sg * kSplineSeg;
+  const int nu = min(kSplineSeg + kSplineWarm, n - 1 - seg0);  // u defined on [0, n-2]
+  for (int k = threadIdx.x; k < nu; k += kSplineThreads) us[k] = uq[seg0 + k];
+  __syncthreads();
+  const int lo = seg0 + threadIdx.x * kSplineChunk;
   const int hi = min(lo + kSplineChunk, n);
-  if (hi == n) yq[n - 1] = mk((R)0, (R)0);
-  const int kst = min(n - 2, hi - 1 + kSplineWarm);
-  double vx = 0., vy = 0.;
-  for (int k = kst; k >= lo; --k) {
-    const double p = ptab[k < 64 ? k : 63];
-    const double2 uk = uq[k];
-    vx = p * vx + uk.x;
-    vy = p * vy + uk.y;
-    if (k < hi) yq[k] = mk((R)vx, (R)vy);
+  if (threadIdx.x < kSplineChunks && lo < n) {
+    const int kst = min(n - 2, hi - 1 + kSplineWarm);
+    double vx = 0., vy = 0.;
+    for (int k = kst; k >= lo; --k) {
+      const double p = ptab[k < 64 ? k : 63];
+      const double2 uk = us[k - seg0];
+      vx = p * vx + uk.x;
+      vy = p * vy + uk.y;
+      if (k < hi) ys[k - seg0] = mk((R)vx, (R)vy);
+    }
+    if (hi == n) ys[n - 1 - seg0] = mk((R)0, (R)0);
   }
+  __syncthreads();
+  const int cnt = min(kSplineSeg, n - seg0);
+  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) yq[seg0 + k] = ys[k];
 }
 
 // splint at x = interpftpad (i - shftf_i) (auxi.c:83-122), then / sig2
@@ -464,76 +528,152 @@ __global__ void __launch_bounds__(256)
 // ------------------------------------------------------------------
 // FStat normalisation and thresholding
 
-// mu_b = sum over the 4096-bin block b of F / (2*4096), auxi.c:228-232
-template <typename R>
-__global__ void __launch_bounds__(256)
-    k_blockmean(const R* __restrict__ F, int bins, int nblk, R* __restrict__ mu) {
-  const int b = blockIdx.x, sidx = blockIdx.y;
-  const R* f = F + (size_t)sidx * bins + (size_t)b * 4096;
+// FStat normalisation (auxi.c:214-240) and thresholding (jobcore.c:659-669)
+// in one kernel.  One CTA per 4096-bin chunk of one spindown: it loads the
+// chunk, forms the block mean mu = sum/(2*4096) with a fixed reduction order
+// (16 loads per thread at stride 256, xor tree per warp, warps in order), so a
+// chunk's mu is bit-identical whichever CTA computes it; chunks beyond the
+// last full block stay unnormalised.  Normalised values go to shared memory,
+// where runs of bins above trl are found; a run produces one candidate at
+// its maximum, ties to the later bin.  The neighbour chunks' means are
+// formed on demand (run starting at the chunk's first bin, or reaching its
+// end), with all threads taking part.
+__device__ __forceinline__ void emit_cand(DevCand* cand, int* ncand, int cap, int task, int ss, int ii,
+                                          double F) {
+  const int slot = atomicAdd(ncand, 1);
+  if (slot < cap) {
+    DevCand d;
+    d.task = task;
+    d.ss = ss;
+    d.ii = ii;
+    d.pad = 0;
+    d.F = F;
+    cand[slot] = d;
+  }
+}
+
+template <typename R> __device__ __forceinline__ R chunk_sum(const R* f, int base, int cnt, R (*red)) {
+  R v[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int i = k * 256 + threadIdx.x;
+    v[k] = i < cnt ? f[base + i] : (R)0;
+  }
   R acc = 0;
 #pragma unroll
-  for (int k = 0; k < 16; ++k) acc += f[k * 256 + threadIdx.x];
+  for (int k = 0; k < 16; ++k) acc += v[k];
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-  __shared__ R red[8];
+  __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    R sum = 0;
-    for (int k = 0; k < 8; ++k) sum += red[k];
-    mu[(size_t)sidx * nblk + b] = sum / (R)(2 * 4096);
-  }
+  R sum = 0;
+  for (int k = 0; k < 8; ++k) sum += red[k];
+  return sum;
 }
 
-template <typename R>
-__device__ __forceinline__ R norm_f(const R* f, const R* m, int i, int nblk, int white) {
-  R v = f[i];
-  if (!white) {
-    const int b = i >> 12;
-    if (b < nblk) v = v / m[b];
-  }
-  return v;
-}
-
-// Runs of consecutive bins above trl produce one candidate at the run's
-// maximum, ties to the later bin (jobcore.c:659-669).
 template <typename R>
 __global__ void __launch_bounds__(256)
-    k_threshold(const R* __restrict__ F, int bins, int nblk, const R* __restrict__ mu, int white,
-                R trl, int nmin, int ss0, int task, DevCand* __restrict__ cand, int* __restrict__ ncand,
-                int cap, R* __restrict__ Fdbg) {
+    k_normthresh(const R* __restrict__ F, int bins, int nblk, int white, R trl, int nmin, int ss0, int task,
+                 DevCand* __restrict__ cand, int* __restrict__ ncand, int cap, R* __restrict__ Fdbg) {
+  __shared__ R sv[4096 + 1];
+  __shared__ R red[8];
   const int c = blockIdx.x, sidx = blockIdx.y;
+  const int nchunk = (bins + 4095) >> 12;
   const R* f = F + (size_t)sidx * bins;
-  const R* m = mu + (size_t)sidx * nblk;
-#pragma unroll 1
+  const int base = c * 4096;
+  const int cnt = min(4096, bins - base);
+  R v[16];
+#pragma unroll
   for (int k = 0; k < 16; ++k) {
-    const int i = c * 4096 + k * 256 + threadIdx.x;
-    if (i >= bins) break;
-    const R v = norm_f(f, m, i, nblk, white);
-    if (Fdbg) Fdbg[(size_t)sidx * bins + i] = v;
-    if (v > trl && (i == 0 || !(norm_f(f, m, i - 1, nblk, white) > trl))) {
-      int ii = i;
-      R Fc = v;
-      for (int j = i + 1; j < bins; ++j) {
-        const R w = norm_f(f, m, j, nblk, white);
+    const int i = k * 256 + threadIdx.x;
+    v[k] = i < cnt ? f[base + i] : (R)0;
+  }
+  const bool norm = !white && c < nblk;
+  R mu = 1;
+  {
+    R acc = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc += v[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    R sum = 0;
+    for (int k = 0; k < 8; ++k) sum += red[k];
+    if (norm) mu = sum / (R)(2 * 4096);
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int i = k * 256 + threadIdx.x;
+    if (i < cnt) {
+      const R x = norm ? v[k] / mu : v[k];
+      sv[i + 1] = x;
+      if (Fdbg) Fdbg[(size_t)sidx * bins + base + i] = x;
+    }
+  }
+  __syncthreads();
+  // value of the bin before the chunk, needed only when the chunk's first
+  // bin is above the threshold
+  if (c > 0 && sv[1] > trl) {
+    const bool pn = !white && c - 1 < nblk;
+    const R s = chunk_sum(f, base - 4096, 4096, red);
+    if (threadIdx.x == 0) sv[0] = pn ? f[base - 1] / (s / (R)(2 * 4096)) : f[base - 1];
+    __syncthreads();
+  }
+  int ii = -1;
+  R Fc = 0;
+  bool pend = false;  // this thread's run reaches the chunk end
+  for (int k = 0; k < 16; ++k) {
+    const int i = threadIdx.x * 16 + k;
+    if (i >= cnt) break;
+    const R x = sv[i + 1];
+    if (x > trl && (base + i == 0 || !(sv[i] > trl))) {
+      int iib = base + i;
+      R Fcb = x;
+      int jj = i + 1;
+      for (; jj < cnt; ++jj) {
+        const R w = sv[jj + 1];
+        if (!(w > trl)) break;
+        if (w >= Fcb) {
+          iib = base + jj;
+          Fcb = w;
+        }
+      }
+      if (jj == cnt && c + 1 < nchunk) {
+        ii = iib;  // continued below
+        Fc = Fcb;
+        pend = true;
+      } else {
+        emit_cand(cand, ncand, cap, task, ss0 + sidx, iib + nmin, Fcb);
+      }
+      k = jj - threadIdx.x * 16;  // bin jj is not above trl (or past the end)
+    }
+  }
+  // follow a run across chunk ends; uniform loop, at most one thread active
+  bool cont = pend;
+  int cur = c;
+  while (__syncthreads_or(cont)) {
+    ++cur;
+    if (cur >= nchunk) break;
+    const int b2 = cur * 4096, n2 = min(4096, bins - b2);
+    const bool pn = !white && cur < nblk;
+    const R s = chunk_sum(f, b2, n2, red);
+    if (cont) {
+      const R m2 = pn ? s / (R)(2 * 4096) : (R)1;
+      int j = 0;
+      for (; j < n2; ++j) {
+        const R w = pn ? f[b2 + j] / m2 : f[b2 + j];
         if (!(w > trl)) break;
         if (w >= Fc) {
-          ii = j;
+          ii = b2 + j;
           Fc = w;
         }
       }
-      const int slot = atomicAdd(ncand, 1);
-      if (slot < cap) {
-        DevCand dcnd;
-        dcnd.task = task;
-        dcnd.ss = ss0 + sidx;
-        dcnd.ii = ii + nmin;
-        dcnd.pad = 0;
-        dcnd.F = (double)Fc;
-        cand[slot] = dcnd;
-      }
+      cont = (j == n2);
     }
   }
+  if (pend) emit_cand(cand, ncand, cap, task, ss0 + sidx, ii + nmin, Fc);
 }
 
 // ------------------------------------------------------------------
@@ -591,20 +731,22 @@ template <typename R, int PM> class EngineT : public Engine {
 
   template <int SIGN, class Loader, class Storer>
   cudaError_t fft(const Geom& g, const void* const* tw, const Loader& ld, const Storer& st, int batch,
-                  cudaStream_t stream, int kind_a, int kind_b) {
+                  cudaStream_t stream, int kind_a, int kind_b, void* ybuf) {
     constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
     const T* t1 = (const T*)tw[0];
     const T* t2 = (const T*)tw[1];
     const T* tlo = (const T*)tw[2];
     const T* thi = (const T*)tw[3];
-    T* yb = (T*)b_.ybuf;
-    const int smA = (E + g.L1) * (int)sizeof(T) + 128;
-    const int smB = (E + g.L2) * (int)sizeof(T);
+    T* yb = (T*)ybuf;
+    const int smA = (g.L1 * tile_pitch<R>(g.C) + g.L1) * (int)sizeof(T) + 128;
+    const int smB = (g.L2 * tile_pitch<R>(g.Rr) + g.L2) * (int)sizeof(T);
     auto ka = k_pass_a<R, SIGN, Loader>;
     auto kb = k_pass_b<R, SIGN, Storer>;
     static bool doneA = false, doneB = false;
-    smem_attr(ka, (E + 1024) * (int)sizeof(T) + 128, doneA);
-    smem_attr(kb, (E + 1024) * (int)sizeof(T), doneB);
+    // largest tile: L1 = 1024 rows of pitch 2C + pad, plus the twiddle table
+    constexpr int smax = (E + 3 * 1024) * (int)sizeof(T) + 128;
+    smem_attr(ka, smax, doneA);
+    smem_attr(kb, smax, doneB);
     dim3 ga(g.L2 >> g.logC, batch), gb(g.L1 >> g.logRr, batch);
     pre(kind_a, batch, stream);
     ka<<<ga, NT, smA, stream>>>(ld, g, t1, tlo, thi, yb);
@@ -626,54 +768,55 @@ template <typename R, int PM> class EngineT : public Engine {
   long long launches() const override { return launches_; }
   size_t real_size() const override { return sizeof(R); }
 
-  cudaError_t prelude(const SkyArgs& sky, cudaStream_t st) override {
+  cudaError_t prelude(const SkyArgs& sky, int slot, cudaStream_t st) override {
     const int N = b_.N, nifo = b_.nifo;
     const int nbx = (N + 255) / 256;
     pre(KK_PRELUDE_MOD, nifo, st);
     k_prelude_mod<R, PM><<<dim3(nbx, nifo), 256, 0, st>>>(
         b_.xDat, b_.DetSSB, (const R*)b_.cosmodf, (const R*)b_.sinmodf, b_.dc, sky, N, (T*)b_.xin,
-        b_.shftf, b_.ph0, b_.ph1, b_.part);
+        b_.shftf, b_.ph0[slot], b_.ph1[slot], b_.part, b_.sums[slot], (R*)b_.sums_r[slot], b_.counter);
     post(st);
-    pre(KK_PRELUDE_SUMS, nifo, st);
-    k_prelude_sums<<<1, 32, 0, st>>>(b_.part, nbx, nifo, b_.dc, b_.sums);
-    post(st);
-    launches_ += 2;
+    launches_ += 1;
     // forward FFT of the zero-padded series (length nfft)
     PlainLoader<R> pl{(const T*)b_.xin, N, N};
     CStore<R> cs1{(T*)b_.spec, b_.nfft, (R)1};
-    cudaError_t e = fft<-1>(gf_, b_.tw_fwd, pl, cs1, nifo, st, KK_FFT_FWD_A, KK_FFT_FWD_B);
+    cudaError_t e = fft<-1>(gf_, b_.tw_fwd, pl, cs1, nifo, st, KK_FFT_FWD_A, KK_FFT_FWD_B, b_.ybuf_pre);
     if (e != cudaSuccess) return e;
     // spectrum remap + backward FFT (length Ninterp), scale interpftpad/Ninterp
     RemapLoader<R> rl{(const T*)b_.spec, b_.nfft, b_.nfft / 2 + 1, b_.Ninterp - b_.nfft};
     CStore<R> cs2{(T*)b_.yint, b_.Ninterp, (R)(2.0 / b_.Ninterp)};
-    e = fft<+1>(gi_, b_.tw_inv, rl, cs2, nifo, st, KK_FFT_INV_A, KK_FFT_INV_B);
+    e = fft<+1>(gi_, b_.tw_inv, rl, cs2, nifo, st, KK_FFT_INV_A, KK_FFT_INV_B, b_.ybuf_pre);
     if (e != cudaSuccess) return e;
     // spline through the first 2N points of each resampled array
     const int n = 2 * N;
-    const int nch = (n + kSplineChunk - 1) / kSplineChunk;
-    const int nthr = nch * 2 * nifo;
+    const int nseg = (n + kSplineSeg - 1) / kSplineSeg;
+    const int smf = kSplineSeg * (int)sizeof(double2) + (kSplineSeg + kSplineWarm + 2) * (int)sizeof(T);
+    const int smb = (kSplineSeg + kSplineWarm) * (int)sizeof(double2) + kSplineSeg * (int)sizeof(T);
+    static bool donef = false, doneb = false;
+    smem_attr(k_spline_fwd<R>, smf, donef);
+    smem_attr(k_spline_bwd<R>, smb, doneb);
     pre(KK_SPLINE_FWD, nifo, st);
-    k_spline_fwd<R><<<(nthr + 127) / 128, 128, 0, st>>>((const T*)b_.yint, b_.Ninterp, (double2*)b_.u,
-                                                        n, nch, 2 * nifo, b_.spline_invp);
+    k_spline_fwd<R><<<nseg * 2 * nifo, kSplineThreads, smf, st>>>((const T*)b_.yint, b_.Ninterp,
+                                                                  (double2*)b_.u, n, nseg, b_.spline_invp);
     post(st);
     pre(KK_SPLINE_BWD, nifo, st);
-    k_spline_bwd<R><<<(nthr + 127) / 128, 128, 0, st>>>((const double2*)b_.u, (T*)b_.y2, n, nch,
-                                                        2 * nifo, b_.spline_p);
+    k_spline_bwd<R><<<nseg * 2 * nifo, kSplineThreads, smb, st>>>((const double2*)b_.u, (T*)b_.y2, n, nseg,
+                                                                  b_.spline_p);
     post(st);
     pre(KK_SPLINT, nifo, st);
     k_splint<R><<<dim3(nbx, nifo), 256, 0, st>>>((const T*)b_.yint, b_.Ninterp, (const T*)b_.y2,
-                                                 b_.shftf, b_.dc, N, (T*)b_.xm);
+                                                 b_.shftf, b_.dc, N, (T*)b_.xm[slot]);
     post(st);
     launches_ += 3;
     return cudaGetLastError();
   }
 
-  cudaError_t spindowns(const SkyArgs& sky, int ss0, int nb, double trl, int white, int s0_flag,
+  cudaError_t spindowns(const SkyArgs& sky, int slot, int ss0, int nb, double trl, int white, int s0_flag,
                         cudaStream_t st, void* Fdbg) override {
     SpinLoader<R, PM> sl;
-    sl.xm = (const T*)b_.xm;
-    sl.ph0 = b_.ph0;
-    sl.ph1 = b_.ph1;
+    sl.xm = (const T*)b_.xm[slot];
+    sl.ph0 = b_.ph0[slot];
+    sl.ph1 = b_.ph1[slot];
     sl.N = b_.N;
     sl.nifo = b_.nifo;
     sl.ss0 = ss0;
@@ -682,20 +825,14 @@ template <typename R, int PM> class EngineT : public Engine {
     sl.M4 = sky.M4;
     sl.M5 = sky.M5;
     sl.s1_0 = sky.s1_0;
-    FstatStore<R> fs{(R*)b_.F, b_.sums, b_.nmin, b_.nmax, b_.bins};
-    cudaError_t e = fft<-1>(gm_, b_.tw_main, sl, fs, nb, st, KK_SPIN_A, KK_SPIN_B);
+    FstatStore<R> fs{(R*)b_.F, (const R*)b_.sums_r[slot], b_.nmin, b_.nmax, b_.bins};
+    cudaError_t e = fft<-1>(gm_, b_.tw_main, sl, fs, nb, st, KK_SPIN_A, KK_SPIN_B, b_.ybuf);
     if (e != cudaSuccess) return e;
-    if (b_.nblk > 0 && !white) {
-      pre(KK_BLOCKMEAN, nb, st);
-      k_blockmean<R><<<dim3(b_.nblk, nb), 256, 0, st>>>((const R*)b_.F, b_.bins, b_.nblk, (R*)b_.mu);
-      post(st);
-      launches_ += 1;
-    }
     const int nchunk = (b_.bins + 4095) / 4096;
     pre(KK_THRESHOLD, nb, st);
-    k_threshold<R><<<dim3(nchunk, nb), 256, 0, st>>>((const R*)b_.F, b_.bins, b_.nblk, (const R*)b_.mu,
-                                                     white, (R)trl, b_.nmin, ss0, sky.task, b_.cand,
-                                                     b_.ncand, b_.cand_cap, (R*)Fdbg);
+    k_normthresh<R><<<dim3(nchunk, nb), 256, 0, st>>>((const R*)b_.F, b_.bins, b_.nblk, white, (R)trl,
+                                                      b_.nmin, ss0, sky.task, b_.cand, b_.ncand,
+                                                      b_.cand_cap, (R*)Fdbg);
     post(st);
     launches_ += 1;
     return cudaGetLastError();

@@ -24,8 +24,10 @@ struct SkyArgs {
   double nS[3];           // unit vector to the source
   double shft1[kMaxDet];  // nS . DetSSB[0..2] per detector
   double cosalfr[kMaxDet], sinalfr[kMaxDet];  // modvir rotated angles
-  double s1_0;            // nn M9 + mm M13 (0 with --nospindown)
-  double M5;              // spindown step (0 with --nospindown)
+  double s1_0;            // nn M9 + mm M13 (0 with --nospindown); over 2 pi
+                          // in the fixed-point phase mode
+  double M5;              // spindown step (0 with --nospindown); over 2 pi
+                          // in the fixed-point phase mode
   double M0, M4;          // frequency step, het1 step
   int task;               // index of the sky point in the current batch
 };
@@ -53,12 +55,18 @@ struct Buffers {
   double* u;                        // [nifo][2][2N] double2
   void* y2;                         // [nifo][2][2N] Real complex
   double* shftf;                    // [nifo][N]
-  void* ph0;                        // phase coefficients [nifo][N] (mode dependent)
-  void* ph1;
-  void* xm;                         // [nifo][2][N] Real complex
+  // per-sky prelude outputs, double-buffered (slot 0/1) so that the prelude
+  // of one sky point runs while the spindowns of the previous one read the
+  // other slot
+  void* ph0[2];                     // phase coefficients [nifo][N] (mode dependent)
+  void* ph1[2];
+  void* xm[2];                      // [nifo][2][N] Real complex
+  double* sums[2];                  // aa, bb, 1/aa, 1/bb
+  void* sums_r[2];                  // 1/aa, 1/bb in the working precision
   double* part;                     // partial sums of a^2, b^2
-  double* sums;                     // aa, bb, 1/aa, 1/bb
-  void* ybuf;                       // FFT intermediate, max(sbatch*2*nfftf, nifo*2*Ninterp)
+  void* ybuf_pre;                   // FFT intermediate of the prelude, nifo*2*Ninterp
+  unsigned int* counter;            // CTA completion counter of the prelude (kept 0)
+  void* ybuf;                       // FFT intermediate of the spindown loop, sbatch*2*nfftf
   void* F;                          // [sbatch][bins] Real
   void* mu;                         // [sbatch][nblk] Real
   DevCand* cand;
@@ -95,12 +103,14 @@ class Engine {
  public:
   Prof* prof = nullptr;  // owned by the context
   virtual ~Engine() {}
-  // Enqueues the per-sky prelude (jobcore.c:270-393) on `st`.
-  virtual cudaError_t prelude(const SkyArgs& sky, cudaStream_t st) = 0;
-  // Enqueues spindowns ss0 .. ss0+nb-1 (nb <= sbatch): phase modulation,
-  // FFT, F-statistic, normalisation, threshold and candidate compaction.
-  // Fdbg (optional): normalised F of the batch, [nb][bins] Real.
-  virtual cudaError_t spindowns(const SkyArgs& sky, int ss0, int nb, double trl, int white,
+  // Enqueues the per-sky prelude (jobcore.c:270-393) on `st`, outputs to
+  // prelude slot `slot`.
+  virtual cudaError_t prelude(const SkyArgs& sky, int slot, cudaStream_t st) = 0;
+  // Enqueues spindowns ss0 .. ss0+nb-1 (nb <= sbatch) reading prelude slot
+  // `slot`: phase modulation, FFT, F-statistic, normalisation, threshold
+  // and candidate compaction.  Fdbg (optional): normalised F of the batch,
+  // [nb][bins] Real.
+  virtual cudaError_t spindowns(const SkyArgs& sky, int slot, int ss0, int nb, double trl, int white,
                                 int s0_flag, cudaStream_t st, void* Fdbg) = 0;
   virtual long long launches() const = 0;
   virtual size_t real_size() const = 0;

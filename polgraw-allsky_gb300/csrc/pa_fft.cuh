@@ -96,61 +96,146 @@ template <int SIGN, int RAD, class T> __device__ __forceinline__ void dftr(T* v)
   else dft8<SIGN>(v);
 }
 
-// One Stockham stage of radix RAD over Q interleaved sequences of length L.
-// PER butterflies per thread (PER * RAD * NT == Q * L).
-template <int SIGN, int RAD, int PER, int NT, class T>
-__device__ __forceinline__ void fft_stage(T* s, const T* tw, int L, int logL, int Ns, int logNs,
-                                          int logQ) {
-  const int Qmask = (1 << logQ) - 1;
-  const int LR = L / RAD;
-  const int logRAD = RAD == 2 ? 1 : (RAD == 4 ? 2 : 3);
-  // twiddle index step L/(Ns*RAD)
-  const int twshift = logL - logNs - logRAD;
-  T v[PER][RAD];
-  int jj[PER];
-#pragma unroll
-  for (int it = 0; it < PER; ++it) {
-    const int b = threadIdx.x + it * NT;
-    const int q = b & Qmask, j = b >> logQ;
-    jj[it] = j;
-#pragma unroll
-    for (int r = 0; r < RAD; ++r) v[it][r] = s[((j + r * LR) << logQ) + q];
-    if (Ns > 1) {
-      const int k = j & (Ns - 1);
-#pragma unroll
-      for (int r = 1; r < RAD; ++r) v[it][r] = cmul(v[it][r], tw[(k * r) << twshift]);
-    }
-    dftr<SIGN, RAD>(v[it]);
+// Shared-memory tile: Cs pair-sequences of length L; element e of
+// pair-sequence c, array arr (0 = a, 1 = b) lives at s[e*P + 2c + arr] with
+// row pitch P = 2*Cs + PADE.  The a/b values of one element are adjacent
+// and moved as one 16-byte access, and the 16-byte row padding keeps both
+// lane mappings conflict-free: consecutive c (rows of 2*Cs elements) and
+// consecutive e (stride P*sizeof(T) = 16 bytes mod 128).
+template <class T> struct Pair;
+template <> struct Pair<float2> {
+  static constexpr int PADE = 2;
+  __device__ __forceinline__ static void ld(const float2* p, float2& a, float2& b) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    a = make_float2(v.x, v.y);
+    b = make_float2(v.z, v.w);
   }
+  __device__ __forceinline__ static void ldg(const float2* p, float2& a, float2& b) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    a = make_float2(v.x, v.y);
+    b = make_float2(v.z, v.w);
+  }
+  __device__ __forceinline__ static void st(float2* p, float2 a, float2 b) {
+    *reinterpret_cast<float4*>(p) = make_float4(a.x, a.y, b.x, b.y);
+  }
+};
+template <> struct Pair<double2> {
+  static constexpr int PADE = 1;
+  __device__ __forceinline__ static void ld(const double2* p, double2& a, double2& b) {
+    a = p[0];
+    b = p[1];
+  }
+  __device__ __forceinline__ static void ldg(const double2* p, double2& a, double2& b) {
+    a = __ldg(p);
+    b = __ldg(p + 1);
+  }
+  __device__ __forceinline__ static void st(double2* p, double2 a, double2 b) {
+    p[0] = a;
+    p[1] = b;
+  }
+};
+
+template <int RAD> struct LogR { static constexpr int v = RAD == 2 ? 1 : (RAD == 4 ? 2 : 3); };
+
+// Reads the RAD inputs of one pair-butterfly of a Stockham stage from shared
+// memory, applies the stage twiddles W_{Ns RAD}^{k r} and transforms both
+// arrays.  Lane mapping: JFAST -> consecutive j, else consecutive c.
+template <int SIGN, int RAD, int NT, bool JFAST, class T>
+__device__ __forceinline__ void stage_load(const T* s, const T* tw, int logL, int Ns, int logNs, int logCs,
+                                           int P, int it, int& j, int& c, T (&va)[RAD], T (&vb)[RAD]) {
+  const int lr = LogR<RAD>::v;
+  const int logLR = logL - lr;
+  const int b = threadIdx.x + it * NT;
+  if (JFAST) {
+    j = b & ((1 << logLR) - 1);
+    c = b >> logLR;
+  } else {
+    c = b & ((1 << logCs) - 1);
+    j = b >> logCs;
+  }
+#pragma unroll
+  for (int r = 0; r < RAD; ++r) Pair<T>::ld(s + (j + (r << logLR)) * P + 2 * c, va[r], vb[r]);
+  if (Ns > 1) {
+    const int k = j & (Ns - 1);
+    const int twshift = logL - logNs - lr;
+#pragma unroll
+    for (int r = 1; r < RAD; ++r) {
+      const T w = tw[(k * r) << twshift];
+      va[r] = cmul(va[r], w);
+      vb[r] = cmul(vb[r], w);
+    }
+  }
+  dftr<SIGN, RAD>(va);
+  dftr<SIGN, RAD>(vb);
+}
+
+// Stockham output position of butterfly j, output r: ((j/Ns)*Ns*RAD + j%Ns) + r*Ns
+template <int RAD> __device__ __forceinline__ int stage_dst(int j, int Ns, int logNs) {
+  return ((j >> logNs) << (logNs + LogR<RAD>::v)) + (j & (Ns - 1));
+}
+
+// A middle stage: shared memory -> registers -> shared memory.
+template <int SIGN, int RAD, int E, int NT, class T>
+__device__ __forceinline__ void stage_mid(T* s, const T* tw, int logL, int Ns, int logNs, int logCs, int P) {
+  constexpr int PPT = E / (2 * RAD * NT);
+  T va[PPT][RAD], vb[PPT][RAD];
+  int jj[PPT], cc[PPT];
+#pragma unroll
+  for (int it = 0; it < PPT; ++it)
+    stage_load<SIGN, RAD, NT, false>(s, tw, logL, Ns, logNs, logCs, P, it, jj[it], cc[it], va[it], vb[it]);
   __syncthreads();
 #pragma unroll
-  for (int it = 0; it < PER; ++it) {
-    const int b = threadIdx.x + it * NT;
-    const int q = b & Qmask, j = jj[it];
-    const int idxD = ((j >> logNs) << (logNs + logRAD)) + (j & (Ns - 1));
+  for (int it = 0; it < PPT; ++it) {
+    const int d = stage_dst<RAD>(jj[it], Ns, logNs);
 #pragma unroll
-    for (int r = 0; r < RAD; ++r) s[((idxD + r * Ns) << logQ) + q] = v[it][r];
+    for (int r = 0; r < RAD; ++r) Pair<T>::st(s + (d + r * Ns) * P + 2 * cc[it], va[it][r], vb[it][r]);
   }
   __syncthreads();
 }
 
-// In-place FFT of 2^logQ interleaved sequences of length L = 2^logL held in
-// shared memory (E = Q*L elements).  tw[m] = exp(SIGN 2 pi i m / L).
-template <int SIGN, int E, int NT, class T>
-__device__ __forceinline__ void cta_fft(T* s, const T* tw, int logL, int logQ) {
-  const int L = 1 << logL;
-  int Ns = 1, logNs = 0;
+// First stage (Ns = 1, no twiddles) from values produced by `src(it, j, c,
+// r, a, b)` in registers, written to shared memory (c-fastest mapping).
+template <int SIGN, int RAD, int E, int NT, class T, class Src>
+__device__ __forceinline__ void stage_first(T* s, int logL, int logCs, int P, const Src& src) {
+  constexpr int PPT = E / (2 * RAD * NT);
+  const int logLR = logL - LogR<RAD>::v;
+#pragma unroll
+  for (int it = 0; it < PPT; ++it) {
+    const int b = threadIdx.x + it * NT;
+    const int c = b & ((1 << logCs) - 1), j = b >> logCs;
+    T va[RAD], vb[RAD];
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) src(j + (r << logLR), c, va[r], vb[r]);
+    dftr<SIGN, RAD>(va);
+    dftr<SIGN, RAD>(vb);
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) Pair<T>::st(s + (j * RAD + r) * P + 2 * c, va[r], vb[r]);
+  }
+  __syncthreads();
+}
+
+// Runs the first stage (radix 2, 4 or 8 by log2(L) mod 3) and the middle
+// radix-8 stages; returns Ns before the last radix-8 stage (= L/8).
+template <int SIGN, int E, int NT, class T, class Src>
+__device__ __forceinline__ int fft_front(T* s, const T* tw, int logL, int logCs, int P, const Src& src,
+                                         int& logNs) {
   const int rem = logL % 3;
+  int Ns;
   if (rem == 1) {
-    fft_stage<SIGN, 2, E / (2 * NT), NT>(s, tw, L, logL, 1, 0, logQ);
+    stage_first<SIGN, 2, E, NT>(s, logL, logCs, P, src);
     Ns = 2;
     logNs = 1;
   } else if (rem == 2) {
-    fft_stage<SIGN, 4, E / (4 * NT), NT>(s, tw, L, logL, 1, 0, logQ);
+    stage_first<SIGN, 4, E, NT>(s, logL, logCs, P, src);
     Ns = 4;
     logNs = 2;
+  } else {
+    stage_first<SIGN, 8, E, NT>(s, logL, logCs, P, src);
+    Ns = 8;
+    logNs = 3;
   }
-  for (; Ns < L; Ns <<= 3, logNs += 3) fft_stage<SIGN, 8, E / (8 * NT), NT>(s, tw, L, logL, Ns, logNs, logQ);
+  for (; logNs + 3 < logL; Ns <<= 3, logNs += 3) stage_mid<SIGN, 8, E, NT>(s, tw, logL, Ns, logNs, logCs, P);
+  return Ns;
 }
 
 // Per-precision tile configuration.
@@ -164,10 +249,16 @@ template <> struct TileCfg<double> {
   static constexpr int NT = 256;
 };
 
+template <typename R> __host__ __device__ constexpr int tile_pitch(int Cs) {
+  return 2 * Cs + Pair<typename CT<R>::T>::PADE;
+}
+
 // Pass A: column FFTs of length L1 over C columns x 2 arrays of one batch
-// item (blockIdx.y), twiddle W_L^{n2 k1}, store to the pass-B tile layout.
-// Loader: __device__ void load2(int batch, int n, T& a, T& b) const, plus an
-// optional per-CTA prologue  __device__ void prologue(int batch, char* smem) const.
+// item (blockIdx.y).  The first radix stage takes its inputs from the
+// loader in registers; the last stage (lanes along k1) applies the
+// inter-pass twiddle W_L^{n2 k1} and writes Y[n2][k1][a|b] straight to
+// global memory, 16 contiguous bytes per lane.
+// Loader: prologue(batch, smem scratch) and load2(batch, n, a, b, scratch).
 template <typename R, int SIGN, class Loader>
 __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
     k_pass_a(const Loader ld, const Geom g, const typename CT<R>::T* __restrict__ tw1,
@@ -176,57 +267,44 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
   typedef typename CT<R>::T T;
   constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int P = tile_pitch<R>(g.C);
   T* s = reinterpret_cast<T*>(smem_raw);
-  T* tws = s + E;
+  T* tws = s + g.L1 * P;
   char* lsm = reinterpret_cast<char*>(tws + g.L1);   // loader scratch
   const int batch = blockIdx.y;
   const int c0 = blockIdx.x << g.logC;
-  const int logQ = g.logC + 1;
   for (int m = threadIdx.x; m < g.L1; m += NT) tws[m] = tw1[m];
   ld.prologue(batch, lsm);
   __syncthreads();
-  const int cmask = g.C - 1;
-  for (int e = threadIdx.x; e < (E >> 1); e += NT) {
-    const int col = e & cmask, n1 = e >> g.logC;
-    T va, vb;
-    ld.load2(batch, (n1 << g.logL2) + c0 + col, va, vb, lsm);
-    s[(n1 << logQ) + col] = va;
-    s[(n1 << logQ) + g.C + col] = vb;
-  }
-  __syncthreads();
-  cta_fft<SIGN, E, NT>(s, tws, g.logL1, logQ);
-  // twiddle + store, V consecutive rows (32 bytes) per item
-  constexpr int V = 32 / sizeof(T);
-  constexpr int logV = V == 4 ? 2 : 1;
-  const int Qmask = (1 << logQ) - 1;
-  const int rgmask = (g.Rr >> logV) - 1, logRg = g.logRr - logV;
+  auto src = [&](int n1, int c, T& a, T& b) { ld.load2(batch, (n1 << g.logL2) + c0 + c, a, b, lsm); };
+  int logNs;
+  const int Ns = fft_front<SIGN, E, NT>(s, tws, g.logL1, g.logC, P, src, logNs);
+  // last radix-8 stage, lanes along j (= k1 mod Ns)
+  constexpr int PPT = E / (2 * 8 * NT);
   const int Lmask = g.L - 1, lomask = (1 << g.twlo_log) - 1;
   T* yb = ybuf + ((size_t)batch << (g.logL + 1));
-  for (int w = threadIdx.x; w < E / V; w += NT) {
-    const int q = w & Qmask, rest = w >> logQ;
-    const int rg = rest & rgmask, t = rest >> logRg;
-    const int arr = q >> g.logC, col = q & cmask;
-    const int n2 = c0 + col;
-    __align__(16) T out[V];
 #pragma unroll
-    for (int v = 0; v < V; ++v) {
-      const int k1 = (t << g.logRr) + (rg << logV) + v;
+  for (int it = 0; it < PPT; ++it) {
+    int j, c;
+    T va[8], vb[8];
+    stage_load<SIGN, 8, NT, true>(s, tws, g.logL1, Ns, logNs, g.logC, P, it, j, c, va, vb);
+    const int n2 = c0 + c;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int k1 = j + r * Ns;
       const int m = (n2 * k1) & Lmask;
       const T W = cmul(__ldg(&twlo[m & lomask]), __ldg(&twhi[m >> g.twlo_log]));
-      out[v] = cmul(s[(k1 << logQ) + q], W);
+      Pair<T>::st(yb + (((size_t)n2 << g.logL1) + k1) * 2, cmul(va[r], W), cmul(vb[r], W));
     }
-    T* dst = yb + ((((size_t)t << g.logL2) + n2) * 2 + arr) * g.Rr + (rg << logV);
-    float4* d4 = reinterpret_cast<float4*>(dst);
-    const float4* o4 = reinterpret_cast<const float4*>(out);
-    d4[0] = o4[0];
-    d4[1] = o4[1];
   }
 }
 
-// Pass B: row FFTs of length L2 over Rr rows x 2 arrays; the storer writes
-// the outputs.  Storer: __device__ void store(int batch, int t, const T* s,
-// const Geom& g) const, called after the FFT with the tile in shared memory
-// (element k2 of sequence q' = arr*Rr + r at s[k2*2Rr + q']).
+// Pass B: row FFTs of length L2 over Rr rows (k1) x 2 arrays.  The first
+// radix stage reads Y[n2][k1][a|b] from global memory (lanes along k1, 16
+// contiguous bytes each); after the last stage every thread hands its
+// outputs X[k1 + L1 k2] for both arrays to the storer:
+//   __device__ void put(int batch, int k1, int k2, T a, T b) const
+// with consecutive lanes on consecutive k1.
 template <typename R, int SIGN, class Storer>
 __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
     k_pass_b(const Storer st, const Geom g, const typename CT<R>::T* __restrict__ tw2,
@@ -234,17 +312,29 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
   typedef typename CT<R>::T T;
   constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int P = tile_pitch<R>(g.Rr);
   T* s = reinterpret_cast<T*>(smem_raw);
-  T* tws = s + E;
-  const int batch = blockIdx.y, t = blockIdx.x;
+  T* tws = s + g.L2 * P;
+  const int batch = blockIdx.y;
+  const int k10 = blockIdx.x << g.logRr;
   for (int m = threadIdx.x; m < g.L2; m += NT) tws[m] = tw2[m];
-  const float4* src = reinterpret_cast<const float4*>(ybuf + ((size_t)batch << (g.logL + 1)) + (size_t)t * E);
-  float4* dst = reinterpret_cast<float4*>(s);
-  constexpr int NV = E * (int)sizeof(T) / 16;
-  for (int i = threadIdx.x; i < NV; i += NT) dst[i] = __ldg(&src[i]);
+  const T* yb = ybuf + ((size_t)batch << (g.logL + 1));
+  auto src = [&](int n2, int rr, T& a, T& b) {
+    Pair<T>::ldg(yb + (((size_t)n2 << g.logL1) + k10 + rr) * 2, a, b);
+  };
   __syncthreads();
-  cta_fft<SIGN, E, NT>(s, tws, g.logL2, g.logRr + 1);
-  st.store(batch, t, s, g);
+  int logNs;
+  const int Ns = fft_front<SIGN, E, NT>(s, tws, g.logL2, g.logRr, P, src, logNs);
+  st.begin(batch, blockIdx.x);
+  constexpr int PPT = E / (2 * 8 * NT);
+#pragma unroll
+  for (int it = 0; it < PPT; ++it) {
+    int j, rr;
+    T va[8], vb[8];
+    stage_load<SIGN, 8, NT, false>(s, tws, g.logL2, Ns, logNs, g.logRr, P, it, j, rr, va, vb);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) st.put(batch, k10 + rr, j + r * Ns, va[r], vb[r], g);
+  }
 }
 
 }  // namespace pa
