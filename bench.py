@@ -157,9 +157,10 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def cpu_baseline(host, tasks, nsky_sample: int, nthreads: int):
+def cpu_baseline(host, tasks, nsky_sample: int, nthreads: int, keep=None):
     """The CPU oracle (all-FP64 C restatement, OpenMP over spindowns) on a
-    bounded sample of the same sky points: templates/s."""
+    bounded sample of the same sky points: templates/s.  With `keep`, the
+    oracle's candidates are appended to it as {(pm,mm,nn,ss,ii): F}."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from pyoracle import Oracle
     dets, nifo = host.detectors()
@@ -172,7 +173,10 @@ def cpu_baseline(host, tasks, nsky_sample: int, nthreads: int):
     t0 = time.perf_counter()
     for (pm, mm, nn) in sample:
         rng.sst = rng.spndr[0]
-        orc.job_core(pm, mm, nn, opts, rng)
+        o = orc.job_core(pm, mm, nn, opts, rng)
+        if keep is not None:
+            for x, r in zip(o["idx"], o["records"]):
+                keep[tuple(int(x[f]) for f in ("pm", "mm", "nn", "ss", "ii"))] = r[4] * r[4] / 2 + 2
     dt = time.perf_counter() - t0
     orc.close()
     return len(sample) * nspin * bins / dt, dt, len(sample)
@@ -188,7 +192,7 @@ def main():
     ap.add_argument("--spindowns", type=int, default=NSPIN_DEFAULT)
     ap.add_argument("--phase", default="fixed", choices=["fixed", "f64", "ff"])
     ap.add_argument("--fp64-sky", type=int, default=48, help="sky points timed in the all-FP64 form")
-    ap.add_argument("--cpu-sky", type=int, default=2, help="sky points in the CPU-baseline sample")
+    ap.add_argument("--cpu-sky", type=int, default=48, help="sky points in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
     args = ap.parse_args()
 
@@ -322,10 +326,22 @@ def main():
         c64.close()
         if rank == 0:
             nth = os.cpu_count() or 1
-            cv, cdt, cn = cpu_baseline(host, tasks, args.cpu_sky, nth)
+            ref = {}
+            cv, cdt, cn = cpu_baseline(host, tasks, args.cpu_sky, nth, keep=ref)
             out["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": nth, "kind": "port",
                                    "sample": "%d sky points x %d spindowns (CPU oracle, OpenMP, %.1f s)" %
                                              (cn, nspin, cdt)}
+            # relative F-statistic error of the mixed form against the FP64 CPU oracle
+            rg, ig, _ = ctx.search_batch(tasks[:cn], opts, rng)
+            got = {tuple(int(x[f]) for f in ("pm", "mm", "nn", "ss", "ii")): r[4] * r[4] / 2 + 2
+                   for x, r in zip(ig, rg)}
+            common = [k for k in ref if k in got]
+            edge = lambda F: abs(F - opts.trl) <= 1e-4 * opts.trl  # noqa: E731
+            out["vs_oracle"] = {"sky_points": cn, "candidates": len(ref),
+                                "fstat_rel_err_max": max([abs(got[k] - ref[k]) / ref[k] for k in common],
+                                                         default=0.0),
+                                "index_mismatches": sum(1 for k in ref if k not in got and not edge(ref[k])) +
+                                sum(1 for k in got if k not in ref and not edge(got[k]))}
     if rank == 0:
         print(json.dumps(out))
     ctx.close()
