@@ -371,8 +371,8 @@ template <typename R> struct CStore {
   int ldo;
   R scale;
   __device__ __forceinline__ void begin(int, int) const {}
-  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, const Geom& g) const {
-    const size_t k = (size_t)k1 + ((size_t)k2 << g.logL1);
+  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, int logL1) const {
+    const size_t k = (size_t)k1 + ((size_t)k2 << logL1);
     out[((size_t)batch * 2 + 0) * ldo + k] = mk(a.x * scale, a.y * scale);
     out[((size_t)batch * 2 + 1) * ldo + k] = mk(b.x * scale, b.y * scale);
   }
@@ -385,8 +385,8 @@ template <typename R> struct FstatStore {
   const R* inv;     // 1/aa, 1/bb in the working precision
   int nmin, nmax, bins;
   __device__ __forceinline__ void begin(int, int) const {}
-  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, const Geom& g) const {
-    const int k = k1 + (k2 << g.logL1);
+  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, int logL1) const {
+    const int k = k1 + (k2 << logL1);
     if (k >= nmin && k < nmax) {
       const R ia = __ldg(&inv[0]), ib = __ldg(&inv[1]);
       F[(size_t)batch * bins + (k - nmin)] = (a.x * a.x + a.y * a.y) * ia + (b.x * b.x + b.y * b.y) * ib;
@@ -584,13 +584,20 @@ __global__ void __launch_bounds__(256)
   const int base = c * 4096;
   const int cnt = min(4096, bins - base);
   R v[16];
+  if (cnt == 4096) {
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const int i = k * 256 + threadIdx.x;
-    v[k] = i < cnt ? f[base + i] : (R)0;
+    for (int k = 0; k < 16; ++k) v[k] = f[base + k * 256 + threadIdx.x];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const int i = k * 256 + threadIdx.x;
+      v[k] = i < cnt ? f[base + i] : (R)0;
+    }
   }
   const bool norm = !white && c < nblk;
-  R mu = 1;
+  // normalised value = F * (1/mu), mu = block sum / (2*4096); within one
+  // ulp of F/mu
+  R imu = 1;
   {
     R acc = 0;
 #pragma unroll
@@ -601,15 +608,20 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
     R sum = 0;
     for (int k = 0; k < 8; ++k) sum += red[k];
-    if (norm) mu = sum / (R)(2 * 4096);
+    if (norm) imu = (R)(2 * 4096) / sum;
   }
+  unsigned above = 0;  // bit k: element k*256 + tid is above the threshold
 #pragma unroll
   for (int k = 0; k < 16; ++k) {
     const int i = k * 256 + threadIdx.x;
-    if (i < cnt) {
-      const R x = norm ? v[k] / mu : v[k];
-      sv[i + 1] = x;
-      if (Fdbg) Fdbg[(size_t)sidx * bins + base + i] = x;
+    v[k] *= imu;
+    if (i < cnt) sv[i + 1] = v[k];
+    above |= (i < cnt && v[k] > trl) ? (1u << k) : 0u;
+  }
+  if (Fdbg) {
+    for (int k = 0; k < 16; ++k) {
+      const int i = k * 256 + threadIdx.x;
+      if (i < cnt) Fdbg[(size_t)sidx * bins + base + i] = v[k];
     }
   }
   __syncthreads();
@@ -618,36 +630,34 @@ __global__ void __launch_bounds__(256)
   if (c > 0 && sv[1] > trl) {
     const bool pn = !white && c - 1 < nblk;
     const R s = chunk_sum(f, base - 4096, 4096, red);
-    if (threadIdx.x == 0) sv[0] = pn ? f[base - 1] / (s / (R)(2 * 4096)) : f[base - 1];
+    if (threadIdx.x == 0) sv[0] = pn ? f[base - 1] * ((R)(2 * 4096) / s) : f[base - 1];
     __syncthreads();
   }
   int ii = -1;
   R Fc = 0;
   bool pend = false;  // this thread's run reaches the chunk end
-  for (int k = 0; k < 16; ++k) {
-    const int i = threadIdx.x * 16 + k;
-    if (i >= cnt) break;
-    const R x = sv[i + 1];
-    if (x > trl && (base + i == 0 || !(sv[i] > trl))) {
-      int iib = base + i;
-      R Fcb = x;
-      int jj = i + 1;
-      for (; jj < cnt; ++jj) {
-        const R w = sv[jj + 1];
-        if (!(w > trl)) break;
-        if (w >= Fcb) {
-          iib = base + jj;
-          Fcb = w;
-        }
+  while (above) {
+    const int k = __ffs(above) - 1;
+    above &= above - 1;
+    const int i = k * 256 + threadIdx.x;
+    if (base + i != 0 && sv[i] > trl) continue;  // not the start of a run
+    int iib = base + i;
+    R Fcb = sv[i + 1];
+    int jj = i + 1;
+    for (; jj < cnt; ++jj) {
+      const R w = sv[jj + 1];
+      if (!(w > trl)) break;
+      if (w >= Fcb) {
+        iib = base + jj;
+        Fcb = w;
       }
-      if (jj == cnt && c + 1 < nchunk) {
-        ii = iib;  // continued below
-        Fc = Fcb;
-        pend = true;
-      } else {
-        emit_cand(cand, ncand, cap, task, ss0 + sidx, iib + nmin, Fcb);
-      }
-      k = jj - threadIdx.x * 16;  // bin jj is not above trl (or past the end)
+    }
+    if (jj == cnt && c + 1 < nchunk) {
+      ii = iib;  // continued below
+      Fc = Fcb;
+      pend = true;
+    } else {
+      emit_cand(cand, ncand, cap, task, ss0 + sidx, iib + nmin, Fcb);
     }
   }
   // follow a run across chunk ends; uniform loop, at most one thread active
@@ -660,10 +670,10 @@ __global__ void __launch_bounds__(256)
     const bool pn = !white && cur < nblk;
     const R s = chunk_sum(f, b2, n2, red);
     if (cont) {
-      const R m2 = pn ? s / (R)(2 * 4096) : (R)1;
+      const R im2 = pn ? (R)(2 * 4096) / s : (R)1;
       int j = 0;
       for (; j < n2; ++j) {
-        const R w = pn ? f[b2 + j] / m2 : f[b2 + j];
+        const R w = f[b2 + j] * im2;
         if (!(w > trl)) break;
         if (w >= Fc) {
           ii = b2 + j;
@@ -729,33 +739,45 @@ template <typename R, int PM> class EngineT : public Engine {
     }
   }
 
-  template <int SIGN, class Loader, class Storer>
-  cudaError_t fft(const Geom& g, const void* const* tw, const Loader& ld, const Storer& st, int batch,
-                  cudaStream_t stream, int kind_a, int kind_b, void* ybuf) {
-    constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
+  template <int SIGN, int LOGL, class Loader, class Storer>
+  cudaError_t fft_l(const void* const* tw, const Loader& ld, const Storer& st, int batch, cudaStream_t stream,
+                    int kind_a, int kind_b, void* ybuf) {
+    typedef FftShape<R, LOGL> G;
+    constexpr int NT = TileCfg<R>::NT;
     const T* t1 = (const T*)tw[0];
     const T* t2 = (const T*)tw[1];
     const T* tlo = (const T*)tw[2];
     const T* thi = (const T*)tw[3];
     T* yb = (T*)ybuf;
-    const int smA = (g.L1 * tile_pitch<R>(g.C) + g.L1) * (int)sizeof(T) + 128;
-    const int smB = (g.L2 * tile_pitch<R>(g.Rr) + g.L2) * (int)sizeof(T);
-    auto ka = k_pass_a<R, SIGN, Loader>;
-    auto kb = k_pass_b<R, SIGN, Storer>;
+    auto ka = k_pass_a<R, SIGN, LOGL, Loader>;
+    auto kb = k_pass_b<R, SIGN, LOGL, Storer>;
     static bool doneA = false, doneB = false;
-    // largest tile: L1 = 1024 rows of pitch 2C + pad, plus the twiddle table
-    constexpr int smax = (E + 3 * 1024) * (int)sizeof(T) + 128;
-    smem_attr(ka, smax, doneA);
-    smem_attr(kb, smax, doneB);
-    dim3 ga(g.L2 >> g.logC, batch), gb(g.L1 >> g.logRr, batch);
+    smem_attr(ka, G::smem_a, doneA);
+    smem_attr(kb, G::smem_b, doneB);
+    dim3 ga(G::L2 >> G::LOGC, batch), gb(G::L1 >> G::LOGRR, batch);
     pre(kind_a, batch, stream);
-    ka<<<ga, NT, smA, stream>>>(ld, g, t1, tlo, thi, yb);
+    ka<<<ga, NT, G::smem_a, stream>>>(ld, t1, tlo, thi, yb);
     post(stream);
     pre(kind_b, batch, stream);
-    kb<<<gb, NT, smB, stream>>>(st, g, t2, yb);
+    kb<<<gb, NT, G::smem_b, stream>>>(st, t2, yb);
     post(stream);
     launches_ += 2;
     return cudaGetLastError();
+  }
+
+  // Dispatch on the transform length (2^12 .. 2^20) to the compile-time
+  // geometry of the passes.
+  template <int SIGN, class Loader, class Storer>
+  cudaError_t fft(const Geom& g, const void* const* tw, const Loader& ld, const Storer& st, int batch,
+                  cudaStream_t stream, int kind_a, int kind_b, void* ybuf) {
+    switch (g.logL) {
+#define PA_FFT_CASE(M) \
+  case M: return fft_l<SIGN, M>(tw, ld, st, batch, stream, kind_a, kind_b, ybuf);
+      PA_FFT_CASE(12) PA_FFT_CASE(13) PA_FFT_CASE(14) PA_FFT_CASE(15) PA_FFT_CASE(16)
+      PA_FFT_CASE(17) PA_FFT_CASE(18) PA_FFT_CASE(19) PA_FFT_CASE(20)
+#undef PA_FFT_CASE
+      default: return cudaErrorInvalidValue;
+    }
   }
 
  public:
