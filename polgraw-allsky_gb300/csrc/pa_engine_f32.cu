@@ -1,14 +1,18 @@
-// pa_engine_f32.cu -- mixed-precision engines (FP32 data, FFTs and
-// F-statistic; FP64 time shifts, prelude phase and spline solve), one per
-// spindown-phase form.
+// pa_engine_f32.cu -- mixed-precision engine (FP32 data, FFTs and
+// F-statistic; FP64 time shifts, prelude phase and spline solve) with the
+// fixed-point spindown phase.  The other phase forms live in their own
+// translation units so that they compile in parallel.
 #include "pa_engine.cuh"
 
 namespace pa {
+Engine* make_engine_f32_f64phase(const Buffers& b);
+Engine* make_engine_f32_ffphase(const Buffers& b);
+
 Engine* make_engine_f32(const Buffers& b, int phase_mode) {
   switch (phase_mode) {
     case PM_FIXED: return new EngineT<float, PM_FIXED>(b);
-    case PM_FF: return new EngineT<float, PM_FF>(b);
-    default: return new EngineT<float, PM_F64>(b);
+    case PM_FF: return make_engine_f32_ffphase(b);
+    default: return make_engine_f32_f64phase(b);
   }
 }
 }  // namespace pa

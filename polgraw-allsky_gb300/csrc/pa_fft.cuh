@@ -139,25 +139,28 @@ template <int RAD> struct LogR { static constexpr int v = RAD == 2 ? 1 : (RAD ==
 
 // Reads the RAD inputs of one pair-butterfly of a Stockham stage from shared
 // memory, applies the stage twiddles W_{Ns RAD}^{k r} and transforms both
-// arrays.  Lane mapping: JFAST -> consecutive j, else consecutive c.
-template <int SIGN, int RAD, int NT, bool JFAST, class T>
-__device__ __forceinline__ void stage_load(const T* s, const T* tw, int logL, int Ns, int logNs, int logCs,
-                                           int P, int it, int& j, int& c, T (&va)[RAD], T (&vb)[RAD]) {
-  const int lr = LogR<RAD>::v;
-  const int logLR = logL - lr;
+// arrays.  Lane mapping: JFAST -> consecutive j, else consecutive c.  All
+// geometry is compile-time (LOGL: log2 of the sequence length, LOGCS: log2
+// of the number of pair-sequences, P: tile row pitch, LOGNS: log2 Ns).
+template <int SIGN, int RAD, int NT, bool JFAST, int LOGL, int LOGCS, int P, int LOGNS, class T>
+__device__ __forceinline__ void stage_load(const T* s, const T* tw, int it, int& j, int& c, T (&va)[RAD],
+                                           T (&vb)[RAD]) {
+  constexpr int lr = LogR<RAD>::v;
+  constexpr int logLR = LOGL - lr;
+  constexpr int Ns = 1 << LOGNS;
   const int b = threadIdx.x + it * NT;
   if (JFAST) {
     j = b & ((1 << logLR) - 1);
     c = b >> logLR;
   } else {
-    c = b & ((1 << logCs) - 1);
-    j = b >> logCs;
+    c = b & ((1 << LOGCS) - 1);
+    j = b >> LOGCS;
   }
 #pragma unroll
   for (int r = 0; r < RAD; ++r) Pair<T>::ld(s + (j + (r << logLR)) * P + 2 * c, va[r], vb[r]);
   if (Ns > 1) {
     const int k = j & (Ns - 1);
-    const int twshift = logL - logNs - lr;
+    constexpr int twshift = LOGL - LOGNS - lr;
 #pragma unroll
     for (int r = 1; r < RAD; ++r) {
       const T w = tw[(k * r) << twshift];
@@ -169,40 +172,37 @@ __device__ __forceinline__ void stage_load(const T* s, const T* tw, int logL, in
   dftr<SIGN, RAD>(vb);
 }
 
-// Stockham output position of butterfly j, output r: ((j/Ns)*Ns*RAD + j%Ns) + r*Ns
-template <int RAD> __device__ __forceinline__ int stage_dst(int j, int Ns, int logNs) {
-  return ((j >> logNs) << (logNs + LogR<RAD>::v)) + (j & (Ns - 1));
-}
-
-// A middle stage: shared memory -> registers -> shared memory.
-template <int SIGN, int RAD, int E, int NT, class T>
-__device__ __forceinline__ void stage_mid(T* s, const T* tw, int logL, int Ns, int logNs, int logCs, int P) {
+// A middle radix-8 stage: shared memory -> registers -> shared memory.
+template <int SIGN, int E, int NT, int LOGL, int LOGCS, int P, int LOGNS, class T>
+__device__ __forceinline__ void stage_mid(T* s, const T* tw) {
+  constexpr int RAD = 8;
   constexpr int PPT = E / (2 * RAD * NT);
+  constexpr int Ns = 1 << LOGNS;
   T va[PPT][RAD], vb[PPT][RAD];
   int jj[PPT], cc[PPT];
 #pragma unroll
   for (int it = 0; it < PPT; ++it)
-    stage_load<SIGN, RAD, NT, false>(s, tw, logL, Ns, logNs, logCs, P, it, jj[it], cc[it], va[it], vb[it]);
+    stage_load<SIGN, RAD, NT, false, LOGL, LOGCS, P, LOGNS>(s, tw, it, jj[it], cc[it], va[it], vb[it]);
   __syncthreads();
 #pragma unroll
   for (int it = 0; it < PPT; ++it) {
-    const int d = stage_dst<RAD>(jj[it], Ns, logNs);
+    const int d = ((jj[it] >> LOGNS) << (LOGNS + 3)) + (jj[it] & (Ns - 1));
 #pragma unroll
     for (int r = 0; r < RAD; ++r) Pair<T>::st(s + (d + r * Ns) * P + 2 * cc[it], va[it][r], vb[it][r]);
   }
   __syncthreads();
 }
 
-// First stage (Ns = 1, no twiddles) from values produced by `src(it, j, c,
-// r, a, b)` in registers, written to shared memory (c-fastest mapping).
-template <int SIGN, int RAD, int E, int NT, class T, class Src>
-__device__ __forceinline__ void stage_first(T* s, int logL, int logCs, int P, const Src& src) {
+// First stage (Ns = 1, no twiddles) from values produced by `src(e, c, a, b)`
+// in registers, written to shared memory (c-fastest mapping).
+template <int SIGN, int RAD, int E, int NT, int LOGL, int LOGCS, int P, class T, class Src>
+__device__ __forceinline__ void stage_first(T* s, const Src& src) {
   constexpr int PPT = E / (2 * RAD * NT);
-  const int logLR = logL - LogR<RAD>::v;
+  constexpr int logLR = LOGL - LogR<RAD>::v;
 #pragma unroll
   for (int it = 0; it < PPT; ++it) {
     const int b = threadIdx.x + it * NT;
-    const int c = b & ((1 << logCs) - 1), j = b >> logCs;
+    const int c = b & ((1 << LOGCS) - 1), j = b >> LOGCS;
     T va[RAD], vb[RAD];
 #pragma unroll
     for (int r = 0; r < RAD; ++r) src(j + (r << logLR), c, va[r], vb[r]);
@@ -214,28 +214,27 @@ __device__ __forceinline__ void stage_first(T* s, int logL, int logCs, int P, co
   __syncthreads();
 }
 
-// Runs the first stage (radix 2, 4 or 8 by log2(L) mod 3) and the middle
-// radix-8 stages; returns Ns before the last radix-8 stage (= L/8).
-template <int SIGN, int E, int NT, class T, class Src>
-__device__ __forceinline__ int fft_front(T* s, const T* tw, int logL, int logCs, int P, const Src& src,
-                                         int& logNs) {
-  const int rem = logL % 3;
-  int Ns;
-  if (rem == 1) {
-    stage_first<SIGN, 2, E, NT>(s, logL, logCs, P, src);
-    Ns = 2;
-    logNs = 1;
-  } else if (rem == 2) {
-    stage_first<SIGN, 4, E, NT>(s, logL, logCs, P, src);
-    Ns = 4;
-    logNs = 2;
-  } else {
-    stage_first<SIGN, 8, E, NT>(s, logL, logCs, P, src);
-    Ns = 8;
-    logNs = 3;
+// Middle stages from log2 Ns = LOGNS up to the last one (recursion on LOGNS).
+template <int SIGN, int E, int NT, int LOGL, int LOGCS, int P, int LOGNS, class T>
+__device__ __forceinline__ void stages_mid(T* s, const T* tw) {
+  if constexpr (LOGNS + 3 < LOGL) {
+    stage_mid<SIGN, E, NT, LOGL, LOGCS, P, LOGNS>(s, tw);
+    stages_mid<SIGN, E, NT, LOGL, LOGCS, P, LOGNS + 3>(s, tw);
   }
-  for (; logNs + 3 < logL; Ns <<= 3, logNs += 3) stage_mid<SIGN, 8, E, NT>(s, tw, logL, Ns, logNs, logCs, P);
-  return Ns;
+}
+
+// Radix of the first stage: 2, 4 or 8 by log2(L) mod 3; the rest are radix 8
+template <int LOGL> struct FirstRadix {
+  static constexpr int rem = LOGL % 3;
+  static constexpr int v = rem == 1 ? 2 : (rem == 2 ? 4 : 8);
+  static constexpr int logv = rem == 1 ? 1 : (rem == 2 ? 2 : 3);
+};
+
+// First stage and middle stages; the last radix-8 stage has Ns = L/8.
+template <int SIGN, int E, int NT, int LOGL, int LOGCS, int P, class T, class Src>
+__device__ __forceinline__ void fft_front(T* s, const T* tw, const Src& src) {
+  stage_first<SIGN, FirstRadix<LOGL>::v, E, NT, LOGL, LOGCS, P>(s, src);
+  stages_mid<SIGN, E, NT, LOGL, LOGCS, P, FirstRadix<LOGL>::logv>(s, tw);
 }
 
 // Per-precision tile configuration.
@@ -253,48 +252,62 @@ template <typename R> __host__ __device__ constexpr int tile_pitch(int Cs) {
   return 2 * Cs + Pair<typename CT<R>::T>::PADE;
 }
 
+// Compile-time tile geometry of a length 2^LOGL transform.
+template <typename R, int LOGL> struct FftShape {
+  static constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
+  static constexpr int logE = E == 8192 ? 13 : 12;
+  static constexpr int LOGL1 = (LOGL + 1) / 2, LOGL2 = LOGL / 2;
+  static constexpr int L1 = 1 << LOGL1, L2 = 1 << LOGL2;
+  static constexpr int LOGC = logE - 1 - LOGL1, C = 1 << LOGC;      // pass-A columns per tile
+  static constexpr int LOGRR = logE - 1 - LOGL2, RR = 1 << LOGRR;   // pass-B rows per tile
+  static constexpr int PA = tile_pitch<R>(C), PB = tile_pitch<R>(RR);
+  static constexpr int smem_a = (L1 * PA + L1) * (int)sizeof(typename CT<R>::T) + 128;
+  static constexpr int smem_b = (L2 * PB + L2) * (int)sizeof(typename CT<R>::T);
+  static_assert(C <= L2 && RR <= L1, "transform too short for the tile");
+};
+
 // Pass A: column FFTs of length L1 over C columns x 2 arrays of one batch
 // item (blockIdx.y).  The first radix stage takes its inputs from the
 // loader in registers; the last stage (lanes along k1) applies the
 // inter-pass twiddle W_L^{n2 k1} and writes Y[n2][k1][a|b] straight to
 // global memory, 16 contiguous bytes per lane.
 // Loader: prologue(batch, smem scratch) and load2(batch, n, a, b, scratch).
-template <typename R, int SIGN, class Loader>
+template <typename R, int SIGN, int LOGL, class Loader>
 __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
-    k_pass_a(const Loader ld, const Geom g, const typename CT<R>::T* __restrict__ tw1,
+    k_pass_a(const Loader ld, const typename CT<R>::T* __restrict__ tw1,
              const typename CT<R>::T* __restrict__ twlo, const typename CT<R>::T* __restrict__ twhi,
              typename CT<R>::T* __restrict__ ybuf) {
   typedef typename CT<R>::T T;
-  constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
+  typedef FftShape<R, LOGL> G;
+  constexpr int E = G::E, NT = G::NT, P = G::PA;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int P = tile_pitch<R>(g.C);
   T* s = reinterpret_cast<T*>(smem_raw);
-  T* tws = s + g.L1 * P;
-  char* lsm = reinterpret_cast<char*>(tws + g.L1);   // loader scratch
+  T* tws = s + G::L1 * P;
+  char* lsm = reinterpret_cast<char*>(tws + G::L1);   // loader scratch
   const int batch = blockIdx.y;
-  const int c0 = blockIdx.x << g.logC;
-  for (int m = threadIdx.x; m < g.L1; m += NT) tws[m] = tw1[m];
+  const int c0 = blockIdx.x << G::LOGC;
+  for (int m = threadIdx.x; m < G::L1; m += NT) tws[m] = tw1[m];
   ld.prologue(batch, lsm);
   __syncthreads();
-  auto src = [&](int n1, int c, T& a, T& b) { ld.load2(batch, (n1 << g.logL2) + c0 + c, a, b, lsm); };
-  int logNs;
-  const int Ns = fft_front<SIGN, E, NT>(s, tws, g.logL1, g.logC, P, src, logNs);
+  auto src = [&](int n1, int c, T& a, T& b) { ld.load2(batch, (n1 << G::LOGL2) + c0 + c, a, b, lsm); };
+  fft_front<SIGN, E, NT, G::LOGL1, G::LOGC, P>(s, tws, src);
   // last radix-8 stage, lanes along j (= k1 mod Ns)
+  constexpr int LOGNS = G::LOGL1 - 3, Ns = 1 << LOGNS;
   constexpr int PPT = E / (2 * 8 * NT);
-  const int Lmask = g.L - 1, lomask = (1 << g.twlo_log) - 1;
-  T* yb = ybuf + ((size_t)batch << (g.logL + 1));
+  constexpr int Lmask = (1 << LOGL) - 1;
+  T* yb = ybuf + ((size_t)batch << (LOGL + 1));
 #pragma unroll
   for (int it = 0; it < PPT; ++it) {
     int j, c;
     T va[8], vb[8];
-    stage_load<SIGN, 8, NT, true>(s, tws, g.logL1, Ns, logNs, g.logC, P, it, j, c, va, vb);
+    stage_load<SIGN, 8, NT, true, G::LOGL1, G::LOGC, P, LOGNS>(s, tws, it, j, c, va, vb);
     const int n2 = c0 + c;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int k1 = j + r * Ns;
       const int m = (n2 * k1) & Lmask;
-      const T W = cmul(__ldg(&twlo[m & lomask]), __ldg(&twhi[m >> g.twlo_log]));
-      Pair<T>::st(yb + (((size_t)n2 << g.logL1) + k1) * 2, cmul(va[r], W), cmul(vb[r], W));
+      const T W = cmul(__ldg(&twlo[m & 1023]), __ldg(&twhi[m >> 10]));
+      Pair<T>::st(yb + (((size_t)n2 << G::LOGL1) + k1) * 2, cmul(va[r], W), cmul(vb[r], W));
     }
   }
 }
@@ -303,37 +316,36 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
 // radix stage reads Y[n2][k1][a|b] from global memory (lanes along k1, 16
 // contiguous bytes each); after the last stage every thread hands its
 // outputs X[k1 + L1 k2] for both arrays to the storer:
-//   __device__ void put(int batch, int k1, int k2, T a, T b) const
+//   __device__ void put(int batch, int k1, int k2, T a, T b, int logL1) const
 // with consecutive lanes on consecutive k1.
-template <typename R, int SIGN, class Storer>
+template <typename R, int SIGN, int LOGL, class Storer>
 __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
-    k_pass_b(const Storer st, const Geom g, const typename CT<R>::T* __restrict__ tw2,
+    k_pass_b(const Storer st, const typename CT<R>::T* __restrict__ tw2,
              const typename CT<R>::T* __restrict__ ybuf) {
   typedef typename CT<R>::T T;
-  constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
+  typedef FftShape<R, LOGL> G;
+  constexpr int E = G::E, NT = G::NT, P = G::PB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int P = tile_pitch<R>(g.Rr);
   T* s = reinterpret_cast<T*>(smem_raw);
-  T* tws = s + g.L2 * P;
+  T* tws = s + G::L2 * P;
   const int batch = blockIdx.y;
-  const int k10 = blockIdx.x << g.logRr;
-  for (int m = threadIdx.x; m < g.L2; m += NT) tws[m] = tw2[m];
-  const T* yb = ybuf + ((size_t)batch << (g.logL + 1));
+  const int k10 = blockIdx.x << G::LOGRR;
+  for (int m = threadIdx.x; m < G::L2; m += NT) tws[m] = tw2[m];
+  const T* yb = ybuf + ((size_t)batch << (LOGL + 1));
   auto src = [&](int n2, int rr, T& a, T& b) {
-    Pair<T>::ldg(yb + (((size_t)n2 << g.logL1) + k10 + rr) * 2, a, b);
+    Pair<T>::ldg(yb + (((size_t)n2 << G::LOGL1) + k10 + rr) * 2, a, b);
   };
   __syncthreads();
-  int logNs;
-  const int Ns = fft_front<SIGN, E, NT>(s, tws, g.logL2, g.logRr, P, src, logNs);
-  st.begin(batch, blockIdx.x);
+  fft_front<SIGN, E, NT, G::LOGL2, G::LOGRR, P>(s, tws, src);
+  constexpr int LOGNS = G::LOGL2 - 3, Ns = 1 << LOGNS;
   constexpr int PPT = E / (2 * 8 * NT);
 #pragma unroll
   for (int it = 0; it < PPT; ++it) {
     int j, rr;
     T va[8], vb[8];
-    stage_load<SIGN, 8, NT, false>(s, tws, g.logL2, Ns, logNs, g.logRr, P, it, j, rr, va, vb);
+    stage_load<SIGN, 8, NT, false, G::LOGL2, G::LOGRR, P, LOGNS>(s, tws, it, j, rr, va, vb);
 #pragma unroll
-    for (int r = 0; r < 8; ++r) st.put(batch, k10 + rr, j + r * Ns, va[r], vb[r], g);
+    for (int r = 0; r < 8; ++r) st.put(batch, k10 + rr, j + r * Ns, va[r], vb[r], G::LOGL1);
   }
 }
 
