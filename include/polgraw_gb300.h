@@ -182,6 +182,23 @@ int pa_debug_prelude(pa_ctx *ctx, int pm, int mm, int nn, double *xDatma,
 int pa_debug_fstat(pa_ctx *ctx, int pm, int mm, int nn, int ss,
                    const pa_opts *opts, double *F);
 
+/* Normalised F-statistic of one template, like pa_debug_fstat() on a
+ * mixed-precision, fixed-point-phase context, but without allocating
+ * anything: for callers that cannot call cudaMalloc (a plugin inside a host
+ * application that owns the GPU memory, code that must not grow its
+ * footprint or synchronise the device with an allocation).  No counterpart
+ * in the reference.  Inputs (settings, detector data) and the output F
+ * (nmax-nmin doubles) are host memory; all device storage is one static
+ * 16 MB array in the library, so sizes are limited to N <= 16384,
+ * nfft <= 16384, nfftf <= 32768, nifo <= 3 (larger ones return PA_ERR_ARG
+ * with the reason in pa_last_error(NULL)).  The first call on a device sets
+ * up the array's device address and should come before any stream
+ * capture.  Calls share the array: they are serialised on the host, and
+ * calls that overlap on the same GPU race. */
+int pa_fstat_noalloc(const pa_settings *sett, const pa_detector *det, int nifo,
+                     int pm, int mm, int nn, int ss, const pa_opts *opts,
+                     int device, double *F);
+
 /* Number of CUDA kernel launches issued by this context so far. */
 long long pa_kernel_launches(const pa_ctx *ctx);
 

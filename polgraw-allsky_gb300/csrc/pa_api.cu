@@ -13,6 +13,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -782,3 +783,268 @@ int pa_debug_fstat(pa_ctx* c, int pm, int mm, int nn, int ss, const pa_opts* o, 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------
+// pa_fstat_noalloc: the normalised F-statistic of one template without any
+// allocation.
+//
+// Some callers cannot allocate device memory: a plugin running inside a
+// host application that owns the GPU memory budget, code that must not
+// grow the process's footprint after start-up, or a caller that runs the
+// search between other work where a cudaMalloc would synchronise the
+// device.  For them this entry point computes what pa_debug_fstat computes
+// for a mixed-precision, fixed-point-phase context -- the normalised F of
+// one (sky point, spindown) -- with every device buffer carved out of one
+// file-scope __device__ array of kNoAllocBytes (16 MB), which every GPU that
+// loads the library holds until the process exits.  Host staging uses
+// static arrays as well; the caller passes the inputs (settings, detector
+// data) and the output array F, all in host memory.
+//
+// Limits: N <= 16384, nfft <= 16384, nfftf <= 32768, nifo <= 3; larger sizes
+// are rejected with PA_ERR_ARG and a message in pa_last_error(NULL).
+// The first call on a device looks up the array's device address
+// (cudaGetSymbolAddress, with that device current); make that first call
+// before any stream capture.  All calls share the array and it keeps the
+// last call's contents: the call clears what must start at zero (the
+// prelude's CTA counter and the candidate count) and overwrites the rest.
+// Calls are serialised on the host by a mutex, but calls that overlap on the
+// GPU (e.g. from another process sharing the device through the same
+// library instance) race on the shared array.
+
+namespace {
+
+constexpr size_t kNoAllocBytes = (size_t)16 << 20;
+constexpr int kNoAllocMaxN = 16384, kNoAllocMaxNfft = 16384, kNoAllocMaxNfftf = 32768, kNoAllocMaxNifo = 3;
+constexpr int kNoAllocCandCap = 1024;
+constexpr int kNoAllocMaxDevices = 64;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_dev_ptr[kNoAllocMaxDevices];
+alignas(64) unsigned char g_noalloc_engine_mem[4096];
+// host staging: the largest twiddle set (tw1 + tw2 + 1024 + L/1024 complex
+// doubles for L <= 2^16) and one real array of N floats
+double g_noalloc_tw[2 * (256 + 256 + 1024 + 64)];
+float g_noalloc_tw_f[2 * (256 + 256 + 1024 + 64)];
+float g_noalloc_real[kNoAllocMaxN];
+float g_noalloc_F[kNoAllocMaxNfftf];
+
+// 256-byte aligned bump layout inside the scratch array
+struct Bump {
+  char* base;
+  size_t off = 0;
+  void* take(size_t bytes) {
+    off = (off + 255) & ~(size_t)255;
+    void* p = base ? base + off : nullptr;
+    off += bytes;
+    return p;
+  }
+};
+
+int noalloc_fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_create_error = buf;
+  return code;
+}
+
+// Lays the buffers of one search out in the scratch (or only sizes them
+// when base == nullptr); returns the bytes used.
+size_t noalloc_layout(char* base, const pa_settings& s, int nifo, pa::Buffers* b, void* tw[3][4], void** Fn) {
+  Bump m{base};
+  const size_t N = s.N, cs = 8;
+  const int bins = s.nmax - s.nmin;
+  memset(b, 0, sizeof(*b));
+  b->xDat = (const double*)m.take(8 * nifo * N);
+  b->DetSSB = (const double*)m.take(8 * nifo * 3 * N);
+  b->cosmodf = m.take(4 * N);
+  b->sinmodf = m.take(4 * N);
+  b->dc = (const pa::DetConst*)m.take(sizeof(pa::DetConst) * pa::kMaxDet);
+  b->spline_invp = (const double*)m.take(8 * 64);
+  b->spline_p = (const double*)m.take(8 * 64);
+  b->xin = m.take(cs * nifo * 2 * N);
+  b->spec = m.take(cs * nifo * 2 * (size_t)s.nfft);
+  b->yint = m.take(cs * nifo * 2 * (size_t)s.Ninterp);
+  b->u = (double*)m.take(16 * nifo * 2 * 2 * N);
+  b->y2 = m.take(cs * nifo * 2 * 2 * N);
+  b->shftf = (double*)m.take(8 * nifo * N);
+  b->ph0[0] = b->ph0[1] = m.take(8 * nifo * N);
+  b->ph1[0] = b->ph1[1] = m.take(8 * nifo * N);
+  b->xm[0] = b->xm[1] = m.take(cs * nifo * 2 * N);
+  b->sums[0] = b->sums[1] = (double*)m.take(8 * 8);
+  b->sums_r[0] = b->sums_r[1] = m.take(8 * 4);
+  b->part = (double*)m.take(8 * 2 * nifo * ((N + 255) / 256));
+  b->counter = (unsigned int*)m.take(16);
+  b->ybuf_pre = m.take(cs * nifo * 2 * (size_t)s.Ninterp);
+  b->ybuf = m.take(cs * 2 * (size_t)s.nfftf);
+  b->F = m.take(4 * (size_t)bins);
+  b->mu = m.take(16);
+  *Fn = m.take(4 * (size_t)bins);  // normalised F (the output)
+  b->cand = (pa::DevCand*)m.take(sizeof(pa::DevCand) * kNoAllocCandCap);
+  b->ncand = (int*)m.take(16);
+  const int lens[3] = {s.nfft, s.Ninterp, s.nfftf};
+  for (int t = 0; t < 3; t++) {
+    int lg = 0;
+    while ((1 << lg) < lens[t]) ++lg;
+    const int n4[4] = {1 << ((lg + 1) / 2), 1 << (lg / 2), 1024, lens[t] / 1024};
+    for (int k = 0; k < 4; k++) tw[t][k] = m.take(cs * (size_t)n4[k]);
+  }
+  b->N = s.N;
+  b->nfft = s.nfft;
+  b->Ninterp = s.Ninterp;
+  b->nfftf = s.nfftf;
+  b->nmin = s.nmin;
+  b->nmax = s.nmax;
+  b->bins = bins;
+  b->nblk = bins / PA_NAVFSTAT;
+  b->nifo = nifo;
+  b->fftpad = s.fftpad;
+  b->sbatch = 1;
+  b->cand_cap = kNoAllocCandCap;
+  for (int k = 0; k < 4; k++) {
+    b->tw_fwd[k] = tw[0][k];
+    b->tw_inv[k] = tw[1][k];
+    b->tw_main[k] = tw[2][k];
+  }
+  return m.off;
+}
+
+// Twiddle tables of length L and sign into the device pointers t[0..3],
+// through the static host staging arrays.
+cudaError_t noalloc_twiddles(int L, int sign, void* const* t, cudaStream_t st) {
+  int lg = 0;
+  while ((1 << lg) < L) ++lg;
+  const int L1 = 1 << ((lg + 1) / 2), L2 = 1 << (lg / 2);
+  const int lens[4] = {L1, L2, 1024, L / 1024};
+  for (int k = 0; k < 4; k++) {
+    for (int j = 0; j < lens[k]; j++) {
+      long num, den;
+      if (k == 0) { num = j; den = L1; }
+      else if (k == 1) { num = j; den = L2; }
+      else if (k == 2) { num = j; den = L; }
+      else { num = (long)j * 1024; den = L; }
+      host_twiddle(num, den, sign, &g_noalloc_tw[2 * j], &g_noalloc_tw[2 * j + 1]);
+      g_noalloc_tw_f[2 * j] = (float)g_noalloc_tw[2 * j];
+      g_noalloc_tw_f[2 * j + 1] = (float)g_noalloc_tw[2 * j + 1];
+    }
+    cudaError_t e = cudaMemcpyAsync(t[k], g_noalloc_tw_f, sizeof(float) * 2 * lens[k], cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(st);  // the staging array is reused
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int pa_fstat_noalloc(const pa_settings* sett, const pa_detector* det, int nifo, int pm, int mm,
+                                int nn, int ss, const pa_opts* o, int device, double* F) {
+  if (!sett || !det || !o || !F) return noalloc_fail(PA_ERR_ARG, "pa_fstat_noalloc: null argument");
+  char why[256];
+  pa_config cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.precision = PA_PREC_MIXED;
+  cfg.phase_mode = PA_PHASE_FIXED;
+  cfg.device = device;
+  if (validate(sett, nifo, &cfg, why, sizeof why)) return noalloc_fail(PA_ERR_ARG, "pa_fstat_noalloc: %s", why);
+  if (sett->N > kNoAllocMaxN || sett->nfft > kNoAllocMaxNfft || sett->nfftf > kNoAllocMaxNfftf ||
+      nifo > kNoAllocMaxNifo)
+    return noalloc_fail(PA_ERR_ARG,
+                        "pa_fstat_noalloc: N=%d nfft=%d nfftf=%d nifo=%d beyond the no-allocation limits "
+                        "(N <= %d, nfft <= %d, nfftf <= %d, nifo <= %d)",
+                        sett->N, sett->nfft, sett->nfftf, nifo, kNoAllocMaxN, kNoAllocMaxNfft, kNoAllocMaxNfftf,
+                        kNoAllocMaxNifo);
+  for (int n = 0; n < nifo; n++)
+    if (!det[n].xDat || !det[n].DetSSB || !(det[n].sig2 > 0))
+      return noalloc_fail(PA_ERR_ARG, "pa_fstat_noalloc: detector %d: missing data or sig2 <= 0", n);
+  if (device < 0 || device >= kNoAllocMaxDevices || device >= pa_device_count())
+    return noalloc_fail(PA_ERR_NODEV, "pa_fstat_noalloc: no CUDA device %d", device);
+  pa::Buffers b;
+  void* tw[3][4];
+  void* Fn = nullptr;
+  const size_t need = noalloc_layout(nullptr, *sett, nifo, &b, tw, &Fn);
+  if (need > kNoAllocBytes)
+    return noalloc_fail(PA_ERR_ARG, "pa_fstat_noalloc: needs %zu bytes of scratch, the array holds %zu", need,
+                        kNoAllocBytes);
+
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return noalloc_fail(PA_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  if (!g_noalloc_dev_ptr[device]) {
+    // one-time set-up on this device: the device address of the array
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return noalloc_fail(PA_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_noalloc_dev_ptr[device] = ptr;
+  }
+  noalloc_layout((char*)g_noalloc_dev_ptr[device], *sett, nifo, &b, tw, &Fn);
+  const cudaStream_t st = cudaStreamPerThread;
+
+  // host-side scalars of the sky point, as job_core computes them
+  pa_ctx c;
+  c.sett = *sett;
+  c.nifo = nifo;
+  c.cfg = cfg;
+  c.fp64 = false;
+  c.rsz = 4;
+  c.dev = device;
+  set_det_consts(&c, det);
+  SkyHost h;
+  sky_setup(&c, pm, mm, nn, o, ss, ss, &h);
+  if (!h.inside) return noalloc_fail(PA_ERR_ARG, "pa_fstat_noalloc: sky point outside the grid disk");
+
+#define NCK(call, what)                                                                    \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return noalloc_fail(PA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e_)); \
+  } while (0)
+  const size_t N = sett->N;
+  for (int n = 0; n < nifo; n++) {
+    NCK(cudaMemcpyAsync((double*)b.xDat + n * N, det[n].xDat, 8 * N, cudaMemcpyHostToDevice, st), "upload");
+    NCK(cudaMemcpyAsync((double*)b.DetSSB + n * 3 * N, det[n].DetSSB, 8 * 3 * N, cudaMemcpyHostToDevice, st),
+        "upload");
+  }
+  NCK(cudaMemcpyAsync((void*)b.dc, c.dc, sizeof(pa::DetConst) * nifo, cudaMemcpyHostToDevice, st), "upload");
+  for (int k = 0; k < 2; k++) {
+    for (size_t i = 0; i < N; i++) {
+      const double omrt = sett->omr * (double)i;  // init.c:450-455
+      g_noalloc_real[i] = (float)(k == 0 ? cos(omrt) : sin(omrt));
+    }
+    NCK(cudaMemcpyAsync((void*)(k == 0 ? b.cosmodf : b.sinmodf), g_noalloc_real, 4 * N, cudaMemcpyHostToDevice,
+                        st), "upload");
+    NCK(cudaStreamSynchronize(st), "upload");  // the staging array is reused
+  }
+  double invp[64], p[64];
+  p[0] = invp[0] = 0.;
+  for (int i = 1; i < 64; i++) {  // auxi.c:71-72
+    invp[i] = 2. / (p[i - 1] + 4.);
+    p[i] = -.5 * invp[i];
+  }
+  NCK(cudaMemcpyAsync((void*)b.spline_invp, invp, sizeof(invp), cudaMemcpyHostToDevice, st), "upload");
+  NCK(cudaMemcpyAsync((void*)b.spline_p, p, sizeof(p), cudaMemcpyHostToDevice, st), "upload");
+  NCK(noalloc_twiddles(sett->nfft, -1, tw[0], st), "twiddles");
+  NCK(noalloc_twiddles(sett->Ninterp, +1, tw[1], st), "twiddles");
+  NCK(noalloc_twiddles(sett->nfftf, -1, tw[2], st), "twiddles");
+  // what must start at zero
+  NCK(cudaMemsetAsync(b.counter, 0, 16, st), "memset");
+  NCK(cudaMemsetAsync(b.ncand, 0, 16, st), "memset");
+
+  pa::Engine* eng = pa::make_engine_f32_fixed_at(g_noalloc_engine_mem, sizeof(g_noalloc_engine_mem), b);
+  if (!eng) return noalloc_fail(PA_ERR_NOMEM, "pa_fstat_noalloc: engine storage too small");
+  const pa::SkyArgs a = sky_args(&c, h, 0);
+  e = eng->prelude(a, 0, st);
+  if (e == cudaSuccess) e = eng->spindowns(a, 0, ss, 1, o->trl, o->white_flag, o->s0_flag, st, Fn);
+  const int bins = sett->nmax - sett->nmin;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g_noalloc_F, Fn, 4 * (size_t)bins, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  eng->~Engine();
+  if (e != cudaSuccess) return noalloc_fail(PA_ERR_CUDA, "pa_fstat_noalloc: %s", cudaGetErrorString(e));
+  for (int i = 0; i < bins; i++) F[i] = g_noalloc_F[i];
+#undef NCK
+  return PA_OK;
+}

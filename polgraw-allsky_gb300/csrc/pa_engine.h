@@ -118,6 +118,7 @@ class Engine {
 
 // Factories (defined in the per-precision translation units).
 Engine* make_engine_f32(const Buffers& b, int phase_mode);
+Engine* make_engine_f32_fixed_at(void* mem, size_t bytes, const Buffers& b);
 Engine* make_engine_f64(const Buffers& b);
 
 // Phase-coefficient bytes per sample for a (precision, phase mode).

@@ -26,7 +26,7 @@ PHASE_NAMES = {"f64": PA_PHASE_F64, "fixed": PA_PHASE_FIXED, "ff": PA_PHASE_FF}
 EXPORTS = [
     "pa_version", "pa_device_count", "pa_create", "pa_set_data", "pa_destroy", "pa_last_error",
     "pa_job_core", "pa_search_batch", "pa_debug_prelude", "pa_debug_fstat", "pa_kernel_launches",
-    "pa_last_call_ms", "pa_set_profiling", "pa_profile_reset", "pa_profile_get",
+    "pa_last_call_ms", "pa_set_profiling", "pa_profile_reset", "pa_profile_get", "pa_fstat_noalloc",
     "pa_host_create", "pa_host_setup", "pa_host_search", "pa_host_main", "pa_host_destroy",
     "pa_host_settings", "pa_host_detectors", "pa_host_range", "pa_host_core_opts",
     "pa_host_config", "pa_host_detector_name",
@@ -107,6 +107,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.pa_profile_reset.restype = None
     lib.pa_profile_get.argtypes = [C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_longlong),
                                    P(C.c_longlong)]
+    lib.pa_fstat_noalloc.argtypes = [P(Settings), P(Detector), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     P(Opts), C.c_int, P(C.c_double)]
     lib.pa_host_create.restype = C.c_void_p
     lib.pa_host_create.argtypes = [C.c_int, P(C.c_char_p), P(C.c_int)]
     lib.pa_host_setup.argtypes = [C.c_void_p]
@@ -327,6 +329,18 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+def fstat_noalloc(settings: Settings, dets, nifo: int, pm: int, mm: int, nn: int, ss: int, opts: Opts,
+                  device: int = 0) -> np.ndarray:
+    """pa_fstat_noalloc: normalised F of one template, no allocation."""
+    lib = load()
+    F = np.zeros(settings.nmax - settings.nmin)
+    rc = lib.pa_fstat_noalloc(C.byref(settings), dets, nifo, pm, mm, nn, ss, C.byref(opts), device,
+                              F.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != PA_OK:
+        raise SearchError("pa_fstat_noalloc failed (%d): %s" % (rc, lib.pa_last_error(None).decode()))
+    return F
 
 
 IDX_DTYPE = np.dtype([("pm", "i4"), ("mm", "i4"), ("nn", "i4"), ("ss", "i4"), ("ii", "i4"), ("F", "f4")])
