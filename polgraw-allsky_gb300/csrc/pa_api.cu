@@ -267,9 +267,8 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   ALLOC(b.y2, cs * nifo * 2 * (size_t)(2 * N));
   ALLOC(b.shftf, sizeof(double) * nifo * (size_t)N);
   for (int k = 0; k < 2; k++) {
-    ALLOC(b.ph0[k], 8 * nifo * (size_t)N);
-    ALLOC(b.ph1[k], 8 * nifo * (size_t)N);
-    ALLOC(b.xm[k], cs * nifo * 2 * (size_t)N);
+    if (c->fp64) ALLOC(b.ph0[k], 8 * nifo * (size_t)N);  // tmp1 (FP32 forms keep it in xm)
+    ALLOC(b.xm[k], 32 * nifo * (size_t)N);  // FP32: one 32-byte record; FP64: two double2
     ALLOC(b.sums[k], sizeof(double) * 8);
     ALLOC(b.sums_r[k], sizeof(double) * 4);
   }
@@ -542,9 +541,12 @@ void sky_setup(const pa_ctx* c, int pm, int mm, int nn, const pa_opts* o, int ss
 pa::SkyArgs sky_args(const pa_ctx* c, const SkyHost& h, int task) {
   pa::SkyArgs a = h.args;
   a.task = task;
+  a.ss_base = 0;
   if (!c->fp64 && c->cfg.phase_mode == PA_PHASE_FIXED) {
-    // the fixed-point phase terms are formed in turns
-    a.s1_0 = a.s1_0 / (2. * M_PI);
+    // the fixed-point phase terms are formed in turns, relative to the
+    // first spindown so that the per-spindown factor is non-negative
+    a.ss_base = h.smin;
+    a.s1_0 = (a.s1_0 + h.smin * a.M5) / (2. * M_PI);
     a.M5 = a.M5 / (2. * M_PI);
   }
   return a;
@@ -730,7 +732,7 @@ int pa_debug_prelude(pa_ctx* c, int pm, int mm, int nn, double* xa, double* xb, 
   cudaError_t e = c->eng->prelude(sky_args(c, h, 0), 0, c->stream_pre);
   if (e != cudaSuccess) return cuda_fail(c, e, "prelude");
   const size_t n = (size_t)c->nifo * 2 * c->sett.N;
-  std::vector<char> buf(n * 2 * c->rsz);
+  std::vector<char> buf(n * 2 * 8);  // FP64 pairs or 32-byte FP32 records
   double sums[4];
   CK(cudaMemcpyAsync(buf.data(), c->b.xm[0], buf.size(), cudaMemcpyDeviceToHost, c->stream_pre), "copy");
   CK(cudaMemcpyAsync(sums, c->b.sums[0], sizeof(sums), cudaMemcpyDeviceToHost, c->stream_pre), "copy");
@@ -741,14 +743,16 @@ int pa_debug_prelude(pa_ctx* c, int pm, int mm, int nn, double* xa, double* xb, 
       double* dst = arr == 0 ? xa : xb;
       if (!dst) continue;
       for (int i = 0; i < N; i++) {
-        const size_t src = ((size_t)d * 2 + arr) * N + i;
         double re, im;
         if (c->fp64) {
+          const size_t src = ((size_t)d * 2 + arr) * N + i;
           re = ((double*)buf.data())[2 * src];
           im = ((double*)buf.data())[2 * src + 1];
         } else {
-          re = ((float*)buf.data())[2 * src];
-          im = ((float*)buf.data())[2 * src + 1];
+          // 32-byte records {xa.re, xa.im, xb.re, xb.im | phase terms}
+          const size_t src = 8 * ((size_t)d * N + i) + 2 * arr;
+          re = ((float*)buf.data())[src];
+          im = ((float*)buf.data())[src + 1];
         }
         dst[2 * ((size_t)d * N + i)] = re;
         dst[2 * ((size_t)d * N + i) + 1] = im;
@@ -872,9 +876,7 @@ size_t noalloc_layout(char* base, const pa_settings& s, int nifo, pa::Buffers* b
   b->u = (double*)m.take(16 * nifo * 2 * 2 * N);
   b->y2 = m.take(cs * nifo * 2 * 2 * N);
   b->shftf = (double*)m.take(8 * nifo * N);
-  b->ph0[0] = b->ph0[1] = m.take(8 * nifo * N);
-  b->ph1[0] = b->ph1[1] = m.take(8 * nifo * N);
-  b->xm[0] = b->xm[1] = m.take(cs * nifo * 2 * N);
+  b->xm[0] = b->xm[1] = m.take(32 * nifo * N);  // 32-byte records
   b->sums[0] = b->sums[1] = (double*)m.take(8 * 8);
   b->sums_r[0] = b->sums_r[1] = m.take(8 * 4);
   b->part = (double*)m.take(8 * 2 * nifo * ((N + 255) / 256));

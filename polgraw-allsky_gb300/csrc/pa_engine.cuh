@@ -124,17 +124,26 @@ __global__ void __launch_bounds__(256)
     const double di = (double)i;
     const double tmp1 = __dadd_rn(__dmul_rn(di, di), __dmul_rn((double)(2 * i), shft));
     const size_t o = (size_t)d * N + i;
-    if (PM == PM_FIXED) {
-      // spindown phase s1(ss) tmp1 = s1_0 tmp1 + ss (M5 tmp1); both terms as
-      // 64-bit fixed-point fractions of a turn (sky.s1_0 and sky.M5 hold the
-      // values divided by 2 pi for this mode)
-      reinterpret_cast<uint64_t*>(ph0)[o] = turns_fixed(sky.s1_0 * tmp1);
-      reinterpret_cast<uint64_t*>(ph1)[o] = turns_fixed(sky.M5 * tmp1);
-    } else if (PM == PM_FF) {
-      const float hi = (float)tmp1;
-      reinterpret_cast<float2*>(ph0)[o] = make_float2(hi, (float)(tmp1 - (double)hi));
-    } else {
+    if (sizeof(R) == 8) {
       reinterpret_cast<double*>(ph0)[o] = tmp1;
+    } else {
+      // FP32 forms: the phase coefficients fill the upper half of the
+      // sample's 32-byte record (the resampled data fill the lower half)
+      uint4 hi16;
+      if (PM == PM_FIXED) {
+        // spindown phase s1(ss) tmp1 = s1(ss_base) tmp1 + (ss - ss_base) (M5 tmp1);
+        // both terms as 64-bit fixed-point fractions of a turn (sky.s1_0
+        // and sky.M5 hold s1(ss_base)/2pi and M5/2pi in this mode)
+        const uint64_t A = turns_fixed(sky.s1_0 * tmp1), B = turns_fixed(sky.M5 * tmp1);
+        hi16 = make_uint4((unsigned)A, (unsigned)(A >> 32), (unsigned)B, (unsigned)(B >> 32));
+      } else if (PM == PM_FF) {
+        const float hi = (float)tmp1;
+        hi16 = make_uint4(__float_as_uint(hi), __float_as_uint((float)(tmp1 - (double)hi)), 0u, 0u);
+      } else {
+        const unsigned long long tb = (unsigned long long)__double_as_longlong(tmp1);
+        hi16 = make_uint4((unsigned)tb, (unsigned)(tb >> 32), 0u, 0u);
+      }
+      reinterpret_cast<uint4*>(ph0)[2 * o + 1] = hi16;
     }
     // prelude phase het0 i + oms shft (jobcore.c:299), FP64
     const double phase = __dadd_rn(__dmul_rn(sky.het0, di), __dmul_rn(sky.oms, shft));
@@ -252,18 +261,22 @@ template <typename R> struct RemapLoader {
 struct SpinCta {
   double het1, s1;
   uint64_t H;
-  long long ss;
+  unsigned ssr;  // ss - ss_base (>= 0), fixed-point form
   float s1h, s1l, h1h, h1l;
 };
+
+// (a * b) mod 2^64 for a 64-bit a and a 32-bit b
+__device__ __forceinline__ uint64_t mul64x32(uint64_t a, unsigned b) {
+  return (uint64_t)(unsigned)a * b + ((uint64_t)((unsigned)(a >> 32) * b) << 32);
+}
 
 // Phase-modulated detector sum of the spindown loop (jobcore.c:455-623):
 //   x_{a,b}[n] = sum_d xm_{a,b,d}[n] exp(-i (het1 n + s1 tmp1_d[n]))  (n < N)
 template <typename R, int PM> struct SpinLoader {
   typedef typename CT<R>::T T;
   const T* xm;       // [nifo][2][N]
-  const void* ph0;
-  const void* ph1;
-  int N, nifo, ss0, s0_flag;
+  const void* ph0;   // FP64 form: tmp1 [nifo][N]; FP32 forms: unused
+  int N, nifo, ss0, ss_base, s0_flag;
   double M0, M4, M5, s1_0;
 
   __device__ __forceinline__ void prologue(int batch, char* sm) const {
@@ -276,7 +289,7 @@ template <typename R, int PM> struct SpinLoader {
       p->het1 = het1;
       p->s1 = s1;
       p->H = (uint64_t)__double2ull_rn(het1 * kTurnsPerRad64);
-      p->ss = s0_flag ? 0 : ss;
+      p->ssr = s0_flag ? 0u : (unsigned)(ss - ss_base);
       p->s1h = (float)s1;
       p->s1l = (float)(s1 - (double)p->s1h);
       p->h1h = (float)het1;
@@ -291,11 +304,23 @@ template <typename R, int PM> struct SpinLoader {
     R accx = 0, accy = 0, bccx = 0, bccy = 0;
     double base = 0.;
     uint64_t ibase = 0;
-    if (PM == PM_FIXED) ibase = p->H * (uint64_t)n;
+    if (PM == PM_FIXED) ibase = mul64x32(p->H, (unsigned)n);
     else if (PM == PM_F64) base = p->het1 * (double)n;
     for (int d = 0; d < nifo; ++d) {
       const size_t o = (size_t)d * N + n;
       R sn, cs;
+      T xa, xb;
+      uint4 hi16 = make_uint4(0u, 0u, 0u, 0u);
+      if (sizeof(R) == 8) {
+        xa = xm[((size_t)d * 2 + 0) * N + n];
+        xb = xm[((size_t)d * 2 + 1) * N + n];
+      } else {
+        // one 32-byte record per detector and sample: xa, xb | phase terms
+        const float4 lo16 = __ldg(reinterpret_cast<const float4*>(xm) + 2 * o);
+        hi16 = __ldg(reinterpret_cast<const uint4*>(xm) + 2 * o + 1);
+        xa = mk((R)lo16.x, (R)lo16.y);
+        xb = mk((R)lo16.z, (R)lo16.w);
+      }
       if (sizeof(R) == 8) {
         const double t1 = reinterpret_cast<const double*>(ph0)[o];
         // het1*i + s1*_tmp1 with the reference's rounding (jobcore.c:606)
@@ -305,7 +330,7 @@ template <typename R, int PM> struct SpinLoader {
         sn = (R)sd;
         cs = (R)cd;
       } else if (PM == PM_F64) {
-        const double t1 = reinterpret_cast<const double*>(ph0)[o];
+        const double t1 = __longlong_as_double((long long)(((unsigned long long)hi16.y << 32) | hi16.x));
         const double ph = fma(p->s1, t1, base);
         const double kk = rint(ph * kInvTwoPi);
         double r = fma(-kk, kTwoPiHi, ph);
@@ -315,9 +340,9 @@ template <typename R, int PM> struct SpinLoader {
         sn = (R)sf;
         cs = (R)cf;
       } else if (PM == PM_FIXED) {
-        const uint64_t A = reinterpret_cast<const uint64_t*>(ph0)[o];
-        const uint64_t B = reinterpret_cast<const uint64_t*>(ph1)[o];
-        const uint64_t t = A + (uint64_t)p->ss * B + ibase;
+        const uint64_t A = ((uint64_t)hi16.y << 32) | hi16.x;
+        const uint64_t B = ((uint64_t)hi16.w << 32) | hi16.z;
+        const uint64_t t = A + mul64x32(B, p->ssr) + ibase;
         // top 32 bits as a signed fraction of half a turn: angle = pi * x,
         // x in [-1, 1) (resolution 2^-31 half-turns = 1.5e-9 rad); the
         // 32-bit conversion stays off the FP64 pipe
@@ -328,7 +353,7 @@ template <typename R, int PM> struct SpinLoader {
         cs = (R)cf;
       } else {
         // compensated float-float phase
-        const float2 tt = reinterpret_cast<const float2*>(ph0)[o];
+        const float2 tt = make_float2(__uint_as_float(hi16.x), __uint_as_float(hi16.y));
         float p1 = p->s1h * tt.x;
         float e1 = fmaf(p->s1h, tt.x, -p1);
         e1 = fmaf(p->s1h, tt.y, e1);
@@ -351,8 +376,6 @@ template <typename R, int PM> struct SpinLoader {
         sn = (R)sf;
         cs = (R)cf;
       }
-      const T xa = xm[((size_t)d * 2 + 0) * N + n];
-      const T xb = xm[((size_t)d * 2 + 1) * N + n];
       // x * (cos - i sin)
       accx += xa.x * cs + xa.y * sn;
       accy += xa.y * cs - xa.x * sn;
@@ -507,6 +530,7 @@ __global__ void __launch_bounds__(256)
   const int n = 2 * N;
   const double x = __dmul_rn(2.0, __dsub_rn((double)i, shftf[(size_t)d * N + i]));
   const R is2 = (R)dc[d].inv_sig2;
+  T out[2];
   for (int arr = 0; arr < 2; ++arr) {
     const size_t q = (size_t)d * 2 + arr;
     T v = mk((R)0, (R)0);
@@ -521,7 +545,15 @@ __global__ void __launch_bounds__(256)
       v.x = a * ylo.x + b * yhi.x + (ca * zlo.x + cb * zhi.x) / (R)6;
       v.y = a * ylo.y + b * yhi.y + (ca * zlo.y + cb * zhi.y) / (R)6;
     }
-    xm[q * N + i] = mk(v.x * is2, v.y * is2);
+    out[arr] = mk(v.x * is2, v.y * is2);
+  }
+  if (sizeof(R) == 8) {
+    xm[((size_t)d * 2 + 0) * N + i] = out[0];
+    xm[((size_t)d * 2 + 1) * N + i] = out[1];
+  } else {
+    // lower half of the sample's 32-byte record
+    reinterpret_cast<float4*>(xm)[2 * ((size_t)d * N + i)] =
+        make_float4((float)out[0].x, (float)out[0].y, (float)out[1].x, (float)out[1].y);
   }
 }
 
@@ -796,7 +828,8 @@ template <typename R, int PM> class EngineT : public Engine {
     pre(KK_PRELUDE_MOD, nifo, st);
     k_prelude_mod<R, PM><<<dim3(nbx, nifo), 256, 0, st>>>(
         b_.xDat, b_.DetSSB, (const R*)b_.cosmodf, (const R*)b_.sinmodf, b_.dc, sky, N, (T*)b_.xin,
-        b_.shftf, b_.ph0[slot], b_.ph1[slot], b_.part, b_.sums[slot], (R*)b_.sums_r[slot], b_.counter);
+        b_.shftf, sizeof(R) == 8 ? b_.ph0[slot] : b_.xm[slot], nullptr, b_.part, b_.sums[slot],
+        (R*)b_.sums_r[slot], b_.counter);
     post(st);
     launches_ += 1;
     // forward FFT of the zero-padded series (length nfft)
@@ -838,7 +871,7 @@ template <typename R, int PM> class EngineT : public Engine {
     SpinLoader<R, PM> sl;
     sl.xm = (const T*)b_.xm[slot];
     sl.ph0 = b_.ph0[slot];
-    sl.ph1 = b_.ph1[slot];
+    sl.ss_base = sky.ss_base;
     sl.N = b_.N;
     sl.nifo = b_.nifo;
     sl.ss0 = ss0;

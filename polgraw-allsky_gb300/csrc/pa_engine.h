@@ -29,6 +29,7 @@ struct SkyArgs {
   double M5;              // spindown step (0 with --nospindown); over 2 pi
                           // in the fixed-point phase mode
   double M0, M4;          // frequency step, het1 step
+  int ss_base;            // first spindown of the sky point (fixed-point form)
   int task;               // index of the sky point in the current batch
 };
 
@@ -58,9 +59,11 @@ struct Buffers {
   // per-sky prelude outputs, double-buffered (slot 0/1) so that the prelude
   // of one sky point runs while the spindowns of the previous one read the
   // other slot
-  void* ph0[2];                     // phase coefficients [nifo][N] (mode dependent)
-  void* ph1[2];
-  void* xm[2];                      // [nifo][2][N] Real complex
+  void* ph0[2];                     // FP64 form: tmp1 [nifo][N]
+  void* ph1[2];                     // (unused)
+  void* xm[2];                      // FP32 forms: [nifo][N] 32-byte records
+                                    // {xa, xb | phase terms}; FP64 form:
+                                    // [nifo][2][N] double complex
   double* sums[2];                  // aa, bb, 1/aa, 1/bb
   void* sums_r[2];                  // 1/aa, 1/bb in the working precision
   double* part;                     // partial sums of a^2, b^2
