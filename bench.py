@@ -47,7 +47,7 @@ def load_package():
 
 
 load_package()
-from polgraw_gb300 import synth  # noqa: E402
+from polgraw_gb300 import workloads  # noqa: E402
 
 METRIC = "templates/sec (sky x spindown x bin) mixed vs all-FP64 on GB300 at 1e-4 F-stat err"
 UNIT = "templates/s"
@@ -58,29 +58,7 @@ NSPIN_DEFAULT = 200
 
 def make_workload(root: str, nspin: int):
     """Writes the data set and returns the search command line."""
-    dt, nod, band = 2.0, 2, 666
-    N = synth.nsamples(nod, dt)
-    probe = synth.Dataset(root=root, ident=1, band=band, dt=dt, nod=nod, fftpad=1, M=[], dets=["H1", "L1"], N=N)
-    oms = probe.oms
-    spacing = oms * math.sqrt(math.pi / 2000.)
-    M = synth.grid_matrix(probe.nfft, oms, m5=-1e-9, sky=(spacing, 0.0, 0.0, spacing))
-    ds = synth.write_dataset(root, ident=1, band=band, dt=dt, nod=nod, fftpad=1, dets=["H1", "L1"], M=M)
-    rng = np.random.default_rng(2002)
-    for k in range(5):
-        # uniform in band and spindown range, sky on the first hemisphere
-        while True:
-            delta = float(rng.uniform(-1.2, 1.2))
-            alpha = float(rng.uniform(0, 2 * math.pi))
-            _, pm = synth.ast2lin(alpha, delta)
-            if pm == 1:
-                break
-        synth.inject(ds, f=float(rng.uniform(0.2, 2.9)), fdot=float(rng.uniform(-1.9e-7, 0.0)),
-                     delta=delta, alpha=alpha, snr=float(rng.uniform(8, 15)))
-    nmax = int(math.ceil(1.0 / math.sqrt(math.pi / 2000.))) + 1
-    rpath = os.path.join(root, "range.txt")
-    synth.write_range(rpath, [0, nspin - 1], [-nmax, nmax], [-nmax, nmax], [1, 1])
-    return ["-data", root, "-ident", "1", "-band", str(band), "-dt", "2", "-nod", str(nod), "-range", rpath,
-            "-output", os.path.join(root, "out"), "--nocheckpoint"]
+    return workloads.network(root, nspin)[0]
 
 
 def sky_tasks(host, limit: int):
@@ -148,6 +126,11 @@ def l2_flush():
     del buf
 
 
+# DRAM bytes (read + write) of one spindown pass-A launch (28-29 spindowns,
+# H1+L1, N=86164, nfftf=131072) from an ncu capture of the same kernel
+PASS_A_TRAFFIC = 13.1e6
+
+
 def peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -182,6 +165,67 @@ def cpu_baseline(host, tasks, nsky_sample: int, nthreads: int, keep=None):
     return len(sample) * nspin * bins / dt, dt, len(sample)
 
 
+def run_stress(args, L):
+    """Precision-stress workload (H1+L1, N=258492, nfftf=524288, fdot in
+    [-1e-7, 1e-7)): templates/s of every precision form and the relative
+    F-statistic error of each form on every candidate the all-FP64 CPU oracle
+    finds at the sky points of the three injections (400 spindowns each)."""
+    tmp = tempfile.mkdtemp(prefix="pa_stress_")
+    argv, inj = workloads.stress(tmp, 400)
+    host = L.Host(argv)
+    s = host.settings
+    dets, nifo = host.detectors()
+    opts, rng = host.opts(), host.range
+    bins = s.nmax - s.nmin
+    nspin = rng.spndr[1] - rng.spndr[0] + 1
+    tasks = sky_tasks(host, args.sky if args.sky != NSKY_DEFAULT else 500)
+    inj_sky = [workloads.nearest_sky(host, j) for j in inj]
+    forms = [("mixed-fixed", L.PA_PREC_MIXED, L.PA_PHASE_FIXED), ("mixed-f64phase", L.PA_PREC_MIXED, L.PA_PHASE_F64),
+             ("mixed-ffphase", L.PA_PREC_MIXED, L.PA_PHASE_FF), ("fp64", L.PA_PREC_FP64, L.PA_PHASE_F64)]
+    res, cands = {}, {}
+    for name, prec, ph in forms:
+        ctx = L.Context(s, dets, nifo, precision=prec, phase_mode=ph, device=0)
+        sub = tasks if prec == L.PA_PREC_MIXED else tasks[:args.fp64_sky // 3]
+        for _ in range(max(1, args.warmup)):
+            ctx.search_batch(sub[:4], opts, rng)
+        ms = 0.0
+        for _ in range(args.steps):
+            l2_flush()
+            ctx.search_batch(sub, opts, rng)
+            ms += ctx.last_call_ms()
+        res[name] = {"value": len(sub) * nspin * bins * args.steps / (ms / 1e3), "sky_points": len(sub)}
+        rec, idx, _ = ctx.search_batch(inj_sky, opts, rng)
+        # F from the records' SNR (FP64), as the oracle's
+        cands[name] = {tuple(int(x[f]) for f in ("pm", "mm", "nn", "ss", "ii")): float(r[4] * r[4] / 2 + 2)
+                       for x, r in zip(idx, rec)}
+        ctx.close()
+    keep = {}
+    t_cpu = time.perf_counter()
+    cpu_baseline(host, inj_sky, len(inj_sky), os.cpu_count() or 1, keep=keep)
+    t_cpu = time.perf_counter() - t_cpu
+    per = []
+    for k in sorted(keep):
+        row = {"key": list(k), "F_oracle": keep[k]}
+        for name in cands:
+            row[name] = abs(cands[name][k] - keep[k]) / keep[k] if k in cands[name] else None
+        per.append(row)
+    summary = {}
+    for name in cands:
+        e = [r[name] for r in per if r[name] is not None]
+        summary[name] = {"templates_per_s": res[name]["value"], "sky_points_timed": res[name]["sky_points"],
+                         "rel_err_max": max(e) if e else None, "rel_err_median": statistics.median(e) if e else None,
+                         "candidates_matched": len(e), "candidates_missing": sum(r[name] is None for r in per)}
+    line = {"metric": "templates/sec per precision form and relative F-stat error vs the all-FP64 oracle",
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+            "config": {"workload": "precision stress H1+L1, N=258492 dt=2s, nfft=262144, fftpad=2 (nfftf=524288), "
+                                   "%d sky x %d spindowns, fdot in [-1e-7,1e-7), 3 injections" % (len(tasks), nspin),
+                       "l2": "flushed (256 MB write) before each timed step"},
+            "forms": summary, "oracle_sample": "%d injection sky points x %d spindowns (%.1f s)" %
+                                              (len(inj_sky), nspin, t_cpu),
+            "per_candidate": per}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -194,12 +238,18 @@ def main():
     ap.add_argument("--fp64-sky", type=int, default=48, help="sky points timed in the all-FP64 form")
     ap.add_argument("--cpu-sky", type=int, default=48, help="sky points in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--workload", default="network", choices=["network", "stress"],
+                    help="stress: the N=258492 precision-stress workload, every precision form")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     from polgraw_gb300 import build as pbuild, lib as L
     pbuild.build()
+    if args.workload == "stress":
+        if rank == 0:
+            run_stress(args, L)
+        return
     tmp = tempfile.mkdtemp(prefix="pa_bench_")
     argv = make_workload(tmp, args.spindowns)
     host = L.Host(argv)
@@ -297,7 +347,11 @@ def main():
         achieved = per_unit * items / (ms / 1e3) / 1e9 if name == "spindown_pass_a" else None
         out["roofline"] = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": pk["hbm_gbs"],
                            "unit": "GB/s", "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
-                           "traffic": None, "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
+                           "traffic": PASS_A_TRAFFIC if (name == "spindown_pass_a" and s.N == 86164
+                                                          and nifo == 2) else None,
+                           "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch "
+                                             "(profiles/spindown_pass_a_network_n86164.md)",
+                           "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
                            "avg_launch_ms": ms / max(1, nl), "units_per_launch": items / max(1, nl)}
         out["kernel_share"] = {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
 

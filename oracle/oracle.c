@@ -514,3 +514,263 @@ int ora_job_core(ora_ctx *c, int pm, int mm, int nn, const pa_opts *opts,
   free(tmp1);
   return rc;
 }
+
+/* ------------------------------------------------------------------------
+ * Followup: demodulated network F-statistic (followup/src/followup.c)
+ * ------------------------------------------------------------------------ */
+
+/* Sky set-up of one evaluation point (followup.c:986-1009): sin/cos of
+ * alpha = sgnlo[3] and delta = sgnlo[2], the source unit vector, and
+ * modvir() per detector into aa[n], bb[n]. */
+static void fu_setup(const ora_ctx *c, const double *sgnlo, double nS[3],
+                     double **aa, double **bb) {
+  double sinalt = sin(sgnlo[3]), cosalt = cos(sgnlo[3]);
+  double sindelt = sin(sgnlo[2]), cosdelt = cos(sgnlo[2]);
+  nS[0] = cosalt * cosdelt;
+  nS[1] = sinalt * cosdelt;
+  nS[2] = sindelt;
+  for (int n = 0; n < c->nifo; n++)
+    modvir(sinalt, cosalt, sindelt, cosdelt, c->sett.N, &c->det[n], c->cosmodf,
+           c->sinmodf, aa[n], bb[n]);
+}
+
+/* Fstatnet() (followup.c:413-535): matched filter of every detector at
+ * (f, s, delta, alpha), phase f (i + shft) + s i^2 + (oms + 2 s i) shft
+ * (:460-462), weights 1/sig2 (:496-506), out[0..3] amplitude estimates,
+ * out[4] SNR sqrt(2(F-2)), out[5] = -F, out[6..9] the point, out[10] SNR
+ * from the amplitudes.  cos/sin per sample as the reference's vector calls
+ * (:467-470) with the C library's cos and sin. */
+void ora_fstatnet(ora_ctx *c, const double sgnlo[4], double out[11]) {
+  const int N = c->sett.N, nifo = c->nifo;
+  double nS[3];
+  double *aa[PA_MAX_DETECTORS], *bb[PA_MAX_DETECTORS];
+  double complex *xa[PA_MAX_DETECTORS], *xb[PA_MAX_DETECTORS];
+  for (int n = 0; n < nifo; n++) {
+    aa[n] = (double *)malloc(sizeof(double) * N);
+    bb[n] = (double *)malloc(sizeof(double) * N);
+    xa[n] = (double complex *)malloc(sizeof(double complex) * N);
+    xb[n] = (double complex *)malloc(sizeof(double complex) * N);
+  }
+  fu_setup(c, sgnlo, nS, aa, bb);
+  double *phase = (double *)malloc(sizeof(double) * N);
+  double *cph = (double *)malloc(sizeof(double) * N);
+  double *sph = (double *)malloc(sizeof(double) * N);
+  double complex xasum = 0, xbsum = 0;
+  double sa = 0., sb = 0.;
+  const double oms = c->sett.oms;
+  for (int n = 0; n < nifo; n++) {
+    const double *R = c->DetSSB[n];
+    for (int i = 0; i < N; i++) {
+      double shft = nS[0] * R[i * 3] + nS[1] * R[i * 3 + 1] + nS[2] * R[i * 3 + 2];
+      phase[i] = sgnlo[0] * (double)(i + shft) + (sgnlo[1] * i * i) +
+                 ((oms + 2. * sgnlo[1] * i) * shft);
+    }
+    for (int i = 0; i < N; i++) {
+      cph[i] = cos(phase[i]);
+      sph[i] = sin(phase[i]);
+    }
+    for (int i = 0; i < N; i++) {
+      double complex exph = cph[i] - I * sph[i];
+      xa[n][i] = c->xDat[n][i] * aa[n][i] * exph;
+      xb[n][i] = c->xDat[n][i] * bb[n][i] * exph;
+    }
+  }
+  for (int n = 0; n < nifo; n++) {
+    double at = 0., bt = 0.;
+    const double sig2 = c->det[n].sig2;
+    for (int i = 0; i < N; i++) {
+      at += SQR(aa[n][i]);
+      bt += SQR(bb[n][i]);
+    }
+    for (int i = 0; i < N; i++) {
+      xa[n][i] /= sig2;
+      xb[n][i] /= sig2;
+      xasum += xa[n][i];
+      xbsum += xb[n][i];
+    }
+    sa += at / sig2;
+    sb += bt / sig2;
+  }
+  out[5] = -(((SQR(creal(xasum)) + SQR(cimag(xasum))) / sa) +
+             ((SQR(creal(xbsum)) + SQR(cimag(xbsum))) / sb));
+  out[0] = 2 * creal(xasum) / sa;
+  out[1] = 2 * creal(xbsum) / sb;
+  out[2] = -2 * cimag(xasum) / sa;
+  out[3] = -2 * cimag(xbsum) / sb;
+  out[4] = sqrt(2 * (-out[5] - 2));
+  for (int j = 0; j < 4; j++) out[6 + j] = sgnlo[j];
+  out[10] = sqrt(SQR(2 * creal(xasum)) + SQR(2 * creal(xbsum)) +
+                 SQR(2 * cimag(xasum)) + SQR(2 * cimag(xbsum)));
+  for (int n = 0; n < nifo; n++) {
+    free(aa[n]);
+    free(bb[n]);
+    free(xa[n]);
+    free(xb[n]);
+  }
+  free(phase);
+  free(cph);
+  free(sph);
+}
+
+/* F = -out[5] of ora_fstatnet() and its gradient with respect to
+ * (f, s, delta, alpha) in FP64, by forward differentiation of every factor:
+ *   X_a = sum w a e^{-i phi},  A = sum a^2/sig2  (w = xDat/sig2),
+ *   dF = 2 Re(conj(X_a) dX_a)/A - |X_a|^2 dA/A^2 + (same for b),
+ *   dX_a = sum w (da - i a dphi) e^{-i phi},
+ *   dphi/df = i + shft, dphi/ds = i^2 + 2 i shft,
+ *   dphi/d(delta, alpha) = (f + oms + 2 s i) dshft/d(delta, alpha),
+ * with a, b and their sky derivatives from the modvir() formula
+ * (settings.c:281-325).  The reference gradient of the adjoint tests. */
+double ora_fstatnet_grad(ora_ctx *c, const double sgnlo[4], double grad[4]) {
+  const int N = c->sett.N;
+  const double f = sgnlo[0], s = sgnlo[1], oms = c->sett.oms;
+  const double sd = sin(sgnlo[2]), cd = cos(sgnlo[2]);
+  const double sa_ = sin(sgnlo[3]), ca_ = cos(sgnlo[3]);
+  const double nS[3] = {ca_ * cd, sa_ * cd, sd};
+  const double nD[3] = {-ca_ * sd, -sa_ * sd, cd};      /* d nS / d delta */
+  const double nA[3] = {-sa_ * cd, ca_ * cd, 0.};       /* d nS / d alpha */
+  double complex Xa = 0, Xb = 0, dXa[4] = {0}, dXb[4] = {0};
+  double A = 0, B = 0, dA[4] = {0}, dB[4] = {0};
+  for (int n = 0; n < c->nifo; n++) {
+    const pa_detector *d = &c->det[n];
+    const double *k = d->amod;
+    const double *R = c->DetSSB[n];
+    const double is2 = 1. / d->sig2;
+    const double cosalfr = ca_ * d->cphir + sa_ * d->sphir;
+    const double sinalfr = sa_ * d->cphir - ca_ * d->sphir;
+    const double c2d = cd * cd, c2sd = sd * cd;
+    const double dc2d = -2. * sd * cd, dc2sd = cd * cd - sd * sd;
+    for (int i = 0; i < N; i++) {
+      const double cm = c->cosmodf[i], sm = c->sinmodf[i];
+      const double cc = cosalfr * cm + sinalfr * sm;
+      const double ss = sinalfr * cm - cosalfr * sm;
+      /* d cc/d alpha = -ss, d ss/d alpha = cc */
+      const double c2s = 2. * cc * cc, cs = cc * ss;
+      const double a = k[0] * (2. - c2d) * c2s + k[1] * (2. - c2d) * 2. * cs + k[2] * c2sd * cc +
+                       k[3] * c2sd * ss - k[0] * (2. - c2d) + k[4] * c2d;
+      const double b = k[5] * sd * c2s + k[6] * sd * 2. * cs + k[7] * cd * cc + k[8] * cd * ss -
+                       k[5] * sd;
+      const double a_al = k[0] * (2. - c2d) * (-4. * cs) + k[1] * (2. - c2d) * 2. * (cc * cc - ss * ss) +
+                          k[2] * c2sd * (-ss) + k[3] * c2sd * cc;
+      const double a_de = (-k[0] * c2s - 2. * k[1] * cs + k[0] + k[4]) * dc2d +
+                          (k[2] * cc + k[3] * ss) * dc2sd;
+      const double b_al = k[5] * sd * (-4. * cs) + k[6] * sd * 2. * (cc * cc - ss * ss) +
+                          k[7] * cd * (-ss) + k[8] * cd * cc;
+      const double b_de = cd * (k[5] * c2s + 2. * k[6] * cs - k[5]) - sd * (k[7] * cc + k[8] * ss);
+      const double r0 = R[3 * i], r1 = R[3 * i + 1], r2 = R[3 * i + 2];
+      const double shft = nS[0] * r0 + nS[1] * r1 + nS[2] * r2;
+      const double sh_de = nD[0] * r0 + nD[1] * r1 + nD[2] * r2;
+      const double sh_al = nA[0] * r0 + nA[1] * r1;
+      const double di = (double)i;
+      const double phi = f * (di + shft) + s * di * di + (oms + 2. * s * di) * shft;
+      const double om = f + oms + 2. * s * di;
+      const double dphi[4] = {di + shft, di * di + 2. * di * shft, om * sh_de, om * sh_al};
+      const double da[4] = {0., 0., a_de, a_al}, db[4] = {0., 0., b_de, b_al};
+      const double complex E = cos(phi) - I * sin(phi);
+      const double w = c->xDat[n][i] * is2;
+      Xa += w * a * E;
+      Xb += w * b * E;
+      A += a * a * is2;
+      B += b * b * is2;
+      for (int j = 0; j < 4; j++) {
+        dXa[j] += w * (da[j] - I * a * dphi[j]) * E;
+        dXb[j] += w * (db[j] - I * b * dphi[j]) * E;
+        dA[j] += 2. * a * da[j] * is2;
+        dB[j] += 2. * b * db[j] * is2;
+      }
+    }
+  }
+  const double Pa = SQR(creal(Xa)) + SQR(cimag(Xa)), Pb = SQR(creal(Xb)) + SQR(cimag(Xb));
+  for (int j = 0; j < 4; j++)
+    grad[j] = 2. * creal(conj(Xa) * dXa[j]) / A - Pa * dA[j] / (A * A) +
+              2. * creal(conj(Xb) * dXb[j]) / B - Pb * dB[j] / (B * B);
+  return Pa / A + Pb / B;
+}
+
+/* simplex_extremes() (followup.c:1011-1040) on fx[.][5] = -F. */
+static void fu_extremes(double fx[5][11], int dim, int *ihi, int *ilo, int *inhi) {
+  int hi, lo, nhi;
+  if (fx[0][5] > fx[1][5]) {
+    hi = 0;
+    lo = nhi = 1;
+  } else {
+    hi = 1;
+    lo = nhi = 0;
+  }
+  for (int i = 2; i < dim + 1; i++) {
+    if (fx[i][5] <= fx[lo][5]) lo = i;
+    else if (fx[i][5] > fx[hi][5]) {
+      nhi = hi;
+      hi = i;
+    } else if (fx[i][5] > fx[nhi][5]) nhi = i;
+  }
+  *ihi = hi;
+  *ilo = lo;
+  *inhi = nhi;
+}
+
+/* update_simplex() (followup.c:1055-1087): the point midpoint + scale*line
+ * replaces the worst vertex when it is better than fmax. */
+static int fu_update(ora_ctx *c, double sx[5][4], double fx[5][11], int dim, double fmax,
+                     int ihi, const double *mid, const double *line, double scale, int *nev) {
+  double next[4], f2[11];
+  for (int i = 0; i < dim; i++) next[i] = mid[i] + scale * line[i];
+  ora_fstatnet(c, next, f2);
+  (*nev)++;
+  if (f2[5] < fmax) {
+    for (int i = 0; i < dim; i++) sx[ihi][i] = next[i];
+    for (int j = 0; j < 11; j++) fx[ihi][j] = f2[j];
+    return 1;
+  }
+  return 0;
+}
+
+/* amoeba() (followup.c:1126-1174) with make_simplex (:971-984),
+ * evaluate_simplex (:986-1009), simplex_bearings (:1042-1053),
+ * contract_simplex (:1089-1118) and check_tol (:1120-1124, ZEPS 1e-14,
+ * followup.c:71).  The reference loops until check_tol holds; max_evals
+ * (when > 0) bounds the evaluations.  Returns the number of evaluations;
+ * point[] and out[] receive the best vertex. */
+int ora_amoeba(ora_ctx *c, double point[4], const double pc2[4], double tol, int max_evals,
+               double out[11]) {
+  const int dim = 4;
+  double sx[5][4], fx[5][11], mid[4], line[4];
+  int nev = 0, ihi, ilo, inhi;
+  for (int i = 0; i < dim + 1; i++)
+    for (int j = 0; j < dim; j++) sx[i][j] = point[j];
+  for (int i = 0; i < dim; i++) sx[i][i] = sx[i][i] + pc2[i];
+  for (int i = 0; i < dim + 1; i++, nev++) ora_fstatnet(c, sx[i], fx[i]);
+  for (;;) {
+    fu_extremes(fx, dim, &ihi, &ilo, &inhi);
+    for (int j = 0; j < dim; j++) mid[j] = 0.0;
+    for (int i = 0; i < dim + 1; i++)
+      if (i != ihi)
+        for (int j = 0; j < dim; j++) mid[j] += sx[i][j];
+    for (int j = 0; j < dim; j++) {
+      mid[j] /= dim;
+      line[j] = sx[ihi][j] - mid[j];
+    }
+    {
+      double fmax = fx[ihi][5], fmin = fx[ilo][5];
+      if (fabs(fmax - fmin) < (fabs(fmax) + fabs(fmin)) * tol + 1e-14) break;
+    }
+    if (max_evals > 0 && nev >= max_evals) break;
+    fu_update(c, sx, fx, dim, fx[ihi][5], ihi, mid, line, -1.0, &nev);
+    if (fx[ihi][5] < fx[ilo][5]) {
+      fu_update(c, sx, fx, dim, fx[ihi][5], ihi, mid, line, -2.0, &nev);
+    } else if (fx[ihi][5] > fx[inhi][5]) {
+      if (!fu_update(c, sx, fx, dim, fx[ihi][5], ihi, mid, line, 0.5, &nev)) {
+        for (int i = 0; i < dim + 1; i++) {
+          if (i != ilo) {
+            for (int j = 0; j < dim; j++) sx[i][j] = (sx[ilo][j] + sx[i][j]) * 0.5;
+            ora_fstatnet(c, sx[i], fx[i]);
+            nev++;
+          }
+        }
+      }
+    }
+  }
+  for (int j = 0; j < dim; j++) point[j] = sx[ilo][j];
+  for (int j = 0; j < 11; j++) out[j] = fx[ilo][j];
+  return nev;
+}

@@ -65,6 +65,19 @@ int ora_spindown_range(const pa_settings *sett, int mm, int nn,
                        const pa_opts *opts, const pa_range *s_range,
                        int *smin, int *smax);
 
+/* Followup (followup/src/followup.c).
+ * ora_fstatnet: Fstatnet() at sgnlo = (f, s, delta, alpha) with the sky
+ *   set-up of evaluate_simplex() (followup.c:413-535, 986-1009); out[11] as
+ *   the reference's fstat_out (out[5] = -F).
+ * ora_fstatnet_grad: F and dF/d(f, s, delta, alpha), FP64 forward
+ *   differentiation (the reference gradient of the adjoint tests).
+ * ora_amoeba: the reference simplex (followup.c:1126-1174); max_evals > 0
+ *   bounds the evaluations; returns the number of evaluations. */
+void ora_fstatnet(ora_ctx *c, const double sgnlo[4], double out[11]);
+double ora_fstatnet_grad(ora_ctx *c, const double sgnlo[4], double grad[4]);
+int ora_amoeba(ora_ctx *c, double point[4], const double pc2[4], double tol, int max_evals,
+               double out[11]);
+
 #ifdef __cplusplus
 }
 #endif

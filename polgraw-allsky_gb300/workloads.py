@@ -1,0 +1,82 @@
+"""Synthetic workloads of the benchmark and the large parity cases, written
+in the reference's on-disk layout by polgraw_gb300.synth.
+
+* network(): H1+L1, N=86164 (2 sidereal days at dt=2 s), nfft=131072,
+  fftpad=1, a sky lattice of spacing oms*sqrt(pi/2000) (~2000 points on one
+  hemisphere), 5 injections (SNR 8-15, seed 2002).
+* stress(): H1+L1, N=258492 (6 sidereal days), nfft=262144, fftpad=2
+  (nfftf=524288), spindown step M5=5e-10 over ss in [-nspin/2, nspin/2) so
+  that 400 spindowns span fdot in [-1e-7, 1e-7) (largest spindown phase
+  s1*i^2 ~ 6.7e3 rad), sky lattice of spacing oms*sqrt(pi/500) (~500
+  points), 3 injections (SNR 10-15, seed 2003).
+
+Each returns (command line of the search, list of injections).
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+
+from . import synth
+
+
+def _inject_random(ds, rng, n, *, fdot_lo, fdot_hi, snr_lo, snr_hi, f_lo=0.2, f_hi=2.9):
+    out = []
+    for _ in range(n):
+        while True:
+            delta = float(rng.uniform(-1.2, 1.2))
+            alpha = float(rng.uniform(0, 2 * math.pi))
+            _, pm = synth.ast2lin(alpha, delta)
+            if pm == 1:
+                break
+        inj = dict(f=float(rng.uniform(f_lo, f_hi)), fdot=float(rng.uniform(fdot_lo, fdot_hi)),
+                   delta=delta, alpha=alpha, snr=float(rng.uniform(snr_lo, snr_hi)))
+        synth.inject(ds, **inj)
+        out.append(inj)
+    return out
+
+
+def _lattice(root, *, dt, nod, band, fftpad, m5, npoints, dets=("H1", "L1")):
+    N = synth.nsamples(nod, dt)
+    probe = synth.Dataset(root=root, ident=1, band=band, dt=dt, nod=nod, fftpad=fftpad, M=[],
+                          dets=list(dets), N=N)
+    spacing = probe.oms * math.sqrt(math.pi / npoints)
+    M = synth.grid_matrix(fftpad * probe.nfft, probe.oms, m5=m5, sky=(spacing, 0.0, 0.0, spacing))
+    ds = synth.write_dataset(root, ident=1, band=band, dt=dt, nod=nod, fftpad=fftpad, dets=list(dets), M=M)
+    nmax = int(math.ceil(1.0 / math.sqrt(math.pi / npoints))) + 1
+    return ds, nmax
+
+
+def network(root: str, nspin: int = 200):
+    """The H1+L1 N=86164 network workload (2000 sky x `nspin` spindowns)."""
+    ds, nmax = _lattice(root, dt=2.0, nod=2, band=666, fftpad=1, m5=-1e-9, npoints=2000)
+    inj = _inject_random(ds, np.random.default_rng(2002), 5, fdot_lo=-1.9e-7, fdot_hi=0.0,
+                         snr_lo=8, snr_hi=15)
+    rpath = os.path.join(root, "range.txt")
+    synth.write_range(rpath, [0, nspin - 1], [-nmax, nmax], [-nmax, nmax], [1, 1])
+    return ["-data", root, "-ident", "1", "-band", "666", "-dt", "2", "-nod", "2", "-range", rpath,
+            "-output", os.path.join(root, "out"), "--nocheckpoint"], inj
+
+
+def stress(root: str, nspin: int = 400):
+    """The precision-stress workload: N=258492, nfftf=524288, fdot +-1e-7."""
+    ds, nmax = _lattice(root, dt=2.0, nod=6, band=666, fftpad=2, m5=5e-10, npoints=500)
+    inj = _inject_random(ds, np.random.default_rng(2003), 3, fdot_lo=-0.9e-7, fdot_hi=0.9e-7,
+                         snr_lo=10, snr_hi=15)
+    rpath = os.path.join(root, "range.txt")
+    synth.write_range(rpath, [-(nspin // 2), nspin - nspin // 2 - 1], [-nmax, nmax], [-nmax, nmax], [1, 1])
+    return ["-data", root, "-ident", "1", "-band", "666", "-dt", "2", "-nod", "6", "-range", rpath,
+            "-output", os.path.join(root, "out"), "--nocheckpoint"], inj
+
+
+def nearest_sky(host, inj):
+    """Lattice sky point (pm, mm, nn) nearest to an injection's (delta,
+    alpha), the point where its candidates appear."""
+    s = host.settings
+    be, pm = synth.ast2lin(inj["alpha"], inj["delta"])
+    # al1 = nn M10 + mm M14, al2 = nn M11 + mm M15, with al = be * oms
+    a = np.array([[s.M[10], s.M[14]], [s.M[11], s.M[15]]])
+    nn, mm = np.linalg.solve(a, np.array(be) * s.oms)
+    return (pm, int(round(mm)), int(round(nn)))
