@@ -95,6 +95,40 @@ def _build_ref_variant(subdir: str, out: str, extra: list[str]) -> str:
     return out
 
 
+REF_FOLLOWUP = os.path.join(REF_OUT, "libfollowup_ref.so")
+
+
+def _build_ref_followup() -> str:
+    """The reference followup program's own Fstatnet/evaluate_simplex/amoeba
+    (followup/src/followup.c, followup/src/settings.c and the network
+    search's auxi.c for lin2ast/ast2lin), unmodified, as a shared library
+    driven by oracle/ref_followup_driver.c.  Yeppp! cos/sin come from
+    oracle/shim/yeppp_shim.c (the C library's cos and sin)."""
+    fu = os.path.join(REFERENCE_ROOT, "followup", "src")
+    srcs = [os.path.join(fu, "followup.c"), os.path.join(fu, "settings.c"),
+            os.path.join(NETWORK, "src-cpu", "auxi.c")]
+    mine = [os.path.join(HERE, "ref_followup_driver.c"), os.path.join(HERE, "shim", "yeppp_shim.c"),
+            os.path.join(HERE, "shim", "gsl_shim.c")]
+    if not _newer(REF_FOLLOWUP, srcs + mine):
+        return REF_FOLLOWUP
+    os.makedirs(REF_OUT, exist_ok=True)
+    objdir = os.path.join(REF_OUT, "obj_followup")
+    os.makedirs(objdir, exist_ok=True)
+    inc = ["-I" + os.path.join(HERE, "shim"), "-I" + fu, "-I" + os.path.join(NETWORK, "src-cpu"),
+           "-I" + os.path.join(HERE, "..", "include")]
+    # parity build: no fast-math; -fno-builtin as for the search build
+    cflags = ["-std=gnu11", "-fcommon", "-fPIC", "-O2", "-ffp-contract=off", "-fno-builtin", "-DYEPPP",
+              "-Dmain=followup_reference_main", "-w"] + inc
+    objs = []
+    for k, src in enumerate(srcs + mine):
+        o = os.path.join(objdir, "%d_%s" % (k, os.path.basename(src).replace(".c", ".o")))
+        _run([_CC] + cflags + ["-c", src, "-o", o])
+        objs.append(o)
+    _run([_CC, "-shared", "-o", REF_FOLLOWUP] + objs + ["-lm"])
+    shutil.rmtree(objdir, ignore_errors=True)
+    return REF_FOLLOWUP
+
+
 def build_reference() -> dict:
     """Compile the reference search (serial parity build and OpenMP timing
     build).  Returns {} when the reference checkout is absent."""
@@ -111,6 +145,7 @@ def build_reference() -> dict:
     # timing build: the reference's own optimisation flags (src-openmp/Makefile)
     out["omp"] = _build_ref_variant(
         "src-openmp", REF_OMP, ["-O3", "-ffast-math", "-fopenmp", "-fno-builtin", "-DTIMERS=3"])
+    out["followup"] = _build_ref_followup()
     return out
 
 

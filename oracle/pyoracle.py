@@ -114,3 +114,45 @@ def fft(x: np.ndarray, sign: int) -> np.ndarray:
     if rc:
         raise ValueError("length must be a power of two")
     return out
+
+
+def _fu_bind(lib):
+    P = C.POINTER
+    lib.ora_fstatnet.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
+    lib.ora_fstatnet.restype = None
+    lib.ora_fstatnet_grad.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
+    lib.ora_fstatnet_grad.restype = C.c_double
+    lib.ora_amoeba.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), C.c_double, C.c_int, P(C.c_double)]
+    lib.ora_amoeba.restype = C.c_int
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class FollowupOracle(Oracle):
+    """The followup functions of the oracle (followup.c Fstatnet, the FP64
+    gradient and the simplex) on the same inputs."""
+
+    def __init__(self, settings, dets, nifo: int, nthreads: int = 0):
+        super().__init__(settings, dets, nifo, nthreads)
+        _fu_bind(self.lib)
+
+    def fstatnet(self, sgnlo) -> np.ndarray:
+        p = np.ascontiguousarray(sgnlo, dtype=np.float64)
+        out = np.zeros(11)
+        self.lib.ora_fstatnet(self.o, _dp(p), _dp(out))
+        return out
+
+    def fstatnet_grad(self, sgnlo):
+        p = np.ascontiguousarray(sgnlo, dtype=np.float64)
+        g = np.zeros(4)
+        F = self.lib.ora_fstatnet_grad(self.o, _dp(p), _dp(g))
+        return F, g
+
+    def amoeba(self, point, pc2, tol: float = 1e-7, max_evals: int = 0):
+        p = np.array(point, dtype=np.float64)
+        st = np.ascontiguousarray(pc2, dtype=np.float64)
+        out = np.zeros(11)
+        nev = self.lib.ora_amoeba(self.o, _dp(p), _dp(st), tol, max_evals, _dp(out))
+        return p, out, nev

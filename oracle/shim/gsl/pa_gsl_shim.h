@@ -43,6 +43,7 @@ gsl_permutation *gsl_permutation_alloc(size_t n);
 void gsl_permutation_free(gsl_permutation *p);
 
 int gsl_linalg_LU_decomp(gsl_matrix *A, gsl_permutation *p, int *signum);
+int gsl_linalg_LU_invert(const gsl_matrix *LU, const gsl_permutation *p, gsl_matrix *inv);
 int gsl_linalg_LU_solve(const gsl_matrix *LU, const gsl_permutation *p,
                         const gsl_vector *b, gsl_vector *x);
 

@@ -161,6 +161,20 @@ int gsl_linalg_LU_solve(const gsl_matrix *LU, const gsl_permutation *p,
   return 0;
 }
 
+/* inverse from the LU factors, one column per unit vector */
+int gsl_linalg_LU_invert(const gsl_matrix *LU, const gsl_permutation *p, gsl_matrix *inv) {
+  const size_t n = LU->size1;
+  gsl_vector *e = gsl_vector_alloc(n), *x = gsl_vector_alloc(n);
+  for (size_t j = 0; j < n; j++) {
+    for (size_t i = 0; i < n; i++) gsl_vector_set(e, i, i == j ? 1.0 : 0.0);
+    gsl_linalg_LU_solve(LU, p, e, x);
+    for (size_t i = 0; i < n; i++) inv->data[i * inv->tda + j] = gsl_vector_get(x, i);
+  }
+  gsl_vector_free(e);
+  gsl_vector_free(x);
+  return 0;
+}
+
 gsl_eigen_symmv_workspace *gsl_eigen_symmv_alloc(size_t n) {
   gsl_eigen_symmv_workspace *w = (gsl_eigen_symmv_workspace *)calloc(1, sizeof(*w));
   w->size = n;

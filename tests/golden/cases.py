@@ -53,3 +53,17 @@ CASES = [
          range=[-32, 31, 1, 1, 1, 1, None, None],
          args=["-threshold", "20"]),
 ]
+
+
+# Followup (demodulated F-statistic) cases: data with one injected signal;
+# make_followup_golden.py evaluates the reference followup program's own
+# Fstatnet() at points around the injection and runs its simplex (amoeba)
+# from offset starting points.
+#   fu_h1l1v1   three detectors (H1, L1, V1), N=10771 (1 day at dt=8 s)
+FOLLOWUP_CASES = [
+    dict(name="fu_h1l1v1",
+         data=dict(dets=["H1", "L1", "V1"], dt=8.0, nod=1, band=100, fftpad=1,
+                   grid=dict(m5=-2e-8, sky_scale=0.05)),
+         inject=dict(f=1.0, fdot=-6e-8, delta=0.3, alpha=1.2, snr=25.0),
+         range=[0, 0, 0, 0, 0, 0, None, None]),
+]
