@@ -226,6 +226,91 @@ def run_stress(args, L):
     print(json.dumps(line))
 
 
+def run_followup(args, L):
+    """Followup workload (H1+L1+V1, N=86164, 4096 candidates offset by up to
+    half a peak width from 4 injections): demodulated F-statistic and
+    adjoint-gradient throughput in both forms, gradient ascent of all
+    candidates, the batched reference simplex on the GPU, and the reference
+    simplex (the pinned CPU oracle) on a bounded sample."""
+    tmp = tempfile.mkdtemp(prefix="pa_followup_")
+    argv, inj = workloads.followup(tmp)
+    host = L.Host(argv)
+    s = host.settings
+    dets, nifo = host.detectors()
+    ncand = args.candidates
+    pts, ws, which = workloads.candidates_around(host, inj, ncand)
+    scale = np.median(ws, axis=0)
+    res = {}
+    for name, prec in (("mixed", L.PA_PREC_MIXED), ("fp64", L.PA_PREC_FP64)):
+        fu = L.Followup(s, dets, nifo, precision=prec)
+        for _ in range(max(1, args.warmup)):
+            fu.fstatnet(pts)
+        ms = 0.0
+        for _ in range(args.steps):
+            l2_flush()
+            fu.fstatnet(pts)
+            ms += fu.last_call_ms()
+        gms = 0.0
+        for _ in range(args.steps):
+            l2_flush()
+            F, g = fu.fstatnet_grad(pts)
+            gms += fu.last_call_ms()
+        res[name] = {"fstat_evals_per_s": ncand * args.steps / (ms / 1e3),
+                     "grad_evals_per_s": ncand * args.steps / (gms / 1e3),
+                     "ms_per_batch": ms / args.steps, "grad_ms_per_batch": gms / args.steps,
+                     "F": F, "grad": g}
+        fu.close()
+    # mixed-form gradient against the FP64 form, in peak-width units
+    gm, g64 = res["mixed"].pop("grad"), res["fp64"].pop("grad")
+    Fm, F64 = res["mixed"].pop("F"), res["fp64"].pop("F")
+    gscale = np.abs(scale * g64).max(axis=1)
+    grad_err = float((np.abs(scale * (gm - g64)).max(axis=1) / gscale).max())
+    F_err = float((np.abs(Fm - F64) / F64).max())
+    fu = L.Followup(s, dets, nifo, precision=L.PA_PREC_MIXED)
+    launches0 = fu.launches()
+    t0 = time.perf_counter()
+    p_asc, o_asc, it = fu.ascent(pts, scale, step0=0.25, min_step=1e-3, max_iter=100)
+    t_asc = time.perf_counter() - t0
+    asc_launches = fu.launches() - launches0
+    F0 = -fu.fstatnet(pts)[:, 5]
+    t0 = time.perf_counter()
+    p_sx, o_sx, nev = fu.simplex(pts, 0.5 * scale, tol=1e-7, max_evals=2000)
+    t_sx = time.perf_counter() - t0
+    F_asc, F_sx = -o_asc[:, 5], -o_sx[:, 5]
+    peak = np.array([max(F_asc[which == j].max(), F_sx[which == j].max()) for j in range(len(inj))])
+    reach = lambda Fv: float(np.mean(Fv >= (1 - 1e-3) * peak[which]))
+    # the reference simplex on the CPU: the pinned oracle restatement of
+    # followup.c amoeba, one core, on a bounded sample
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import FollowupOracle
+    ora = FollowupOracle(s, dets, nifo, nthreads=1)
+    ncpu = min(args.cpu_candidates, ncand)
+    t0 = time.perf_counter()
+    cpu_nev = 0
+    for k in range(ncpu):
+        _, _, ne = ora.amoeba(pts[k], 0.5 * scale, 1e-7, 2000)
+        cpu_nev += ne
+    t_cpu = time.perf_counter() - t0
+    ora.close()
+    value = ncand / t_asc
+    line = {"metric": "followup candidates refined per second (gradient ascent, FP32 F-stat + FP64-phase adjoint)",
+            "value": value, "unit": "candidates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "f32+f64phase", "data": "synthetic",
+            "config": {"workload": "followup H1+L1+V1, N=86164 dt=2s, %d candidates offset by U(-0.5,0.5) peak "
+                                   "widths from 4 injections (seed 2005)" % ncand,
+                       "scale": scale.tolist(), "l2": "flushed (256 MB write) before each timed batch"},
+            "forms": res, "mixed_vs_fp64": {"F_rel_err_max": F_err, "grad_rel_err_max_width_units": grad_err},
+            "ascent": {"seconds": t_asc, "iters_mean": float(it.mean()), "F_gain_median": float(np.median(F_asc / F0)),
+                       "reach_peak_frac": reach(F_asc), "gpu_launches": int(asc_launches)},
+            "simplex_gpu": {"seconds": t_sx, "candidates_per_s": ncand / t_sx, "evals_mean": float(nev.mean()),
+                            "reach_peak_frac": reach(F_sx)},
+            "cpu_baseline": {"value": ncpu / t_cpu, "unit": "candidates/s", "cores": 1, "kind": "port",
+                             "sample": "reference simplex (oracle restatement of followup.c amoeba, pinned to it) "
+                                       "on %d candidates, %d evaluations, %.1f s" % (ncpu, cpu_nev, t_cpu)}}
+    fu.close()
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -238,8 +323,11 @@ def main():
     ap.add_argument("--fp64-sky", type=int, default=48, help="sky points timed in the all-FP64 form")
     ap.add_argument("--cpu-sky", type=int, default=48, help="sky points in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--workload", default="network", choices=["network", "stress"],
-                    help="stress: the N=258492 precision-stress workload, every precision form")
+    ap.add_argument("--workload", default="network", choices=["network", "stress", "followup"],
+                    help="stress: the N=258492 precision-stress workload, every precision form; "
+                         "followup: demodulated F-statistic, adjoint, ascent and simplex on 4096 candidates")
+    ap.add_argument("--candidates", type=int, default=4096, help="followup workload: candidates")
+    ap.add_argument("--cpu-candidates", type=int, default=4, help="followup: CPU simplex sample")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -249,6 +337,10 @@ def main():
     if args.workload == "stress":
         if rank == 0:
             run_stress(args, L)
+        return
+    if args.workload == "followup":
+        if rank == 0:
+            run_followup(args, L)
         return
     tmp = tempfile.mkdtemp(prefix="pa_bench_")
     argv = make_workload(tmp, args.spindowns)

@@ -219,6 +219,79 @@ void pa_profile_reset(pa_ctx *ctx);
 int pa_profile_get(const pa_ctx *ctx, int kind, const char **name, double *total_ms,
                    long long *launches, long long *items);
 
+/* ------------------------------------------------------------------------
+ * Followup: the demodulated network F-statistic of followup/src/followup.c
+ * at arbitrary (f, s, delta, alpha), its adjoint gradient, and maximisers.
+ * A point is sgnlo = (f [rad/sample], s [rad/sample^2], delta, alpha [rad])
+ * as in followup.c (sgnlo[0..3]).
+ * ------------------------------------------------------------------------ */
+typedef struct pa_followup pa_followup;
+
+/* Options of pa_followup_ascent(). */
+typedef struct pa_ascent_opts {
+  double scale[4];   /* parameter scales of (f, s, delta, alpha): steps are
+                        measured in these units (e.g. the peak widths
+                        2pi/N, 2pi/N^2 and the sky widths); must be > 0 */
+  double step0;      /* first step length in scale units (<= 0: 0.25) */
+  double min_step;   /* a point stops when its step falls below this
+                        (<= 0: 1e-3) */
+  int max_iter;      /* iteration limit (<= 0: 100) */
+} pa_ascent_opts;
+
+/* Device copies of the data the followup program reads (xDat, DetSSB,
+ * sig2, phir, c1..c9 per detector; followup init.c:326-460) and the
+ * cos/sin(omr i) tables of its init_arrays() (followup init.c:464-475).
+ * Uses sett->N, oms, omr; cfg->precision selects FP32 data with FP64 phase
+ * (PA_PREC_MIXED) or every stage in FP64 (PA_PREC_FP64); cfg->device. */
+pa_followup *pa_followup_create(const pa_settings *sett, const pa_detector *det, int nifo,
+                                const pa_config *cfg, int *status);
+void pa_followup_destroy(pa_followup *fu);
+/* Last error of fu, or of the last failed pa_followup_create() of this
+ * thread when fu is NULL. */
+const char *pa_followup_last_error(const pa_followup *fu);
+
+/* Fstatnet() (followup.c:413-535) with the sky set-up of evaluate_simplex()
+ * (followup.c:986-1009) at n points sgnlo[n][4]; out[n][11] as the
+ * reference's fstat_out: out[0..3] amplitude estimates, out[4] SNR
+ * sqrt(2(F-2)), out[5] = -F, out[6..9] the point, out[10] SNR from the
+ * amplitudes. */
+int pa_fstatnet(pa_followup *fu, const double *sgnlo, int n, double *out);
+
+/* F (= -out[5] of pa_fstatnet) and grad[n][4] = seed[k] dF/d(f, s, delta,
+ * alpha) at n points, by a forward pass and an adjoint (reverse) pass that
+ * recomputes the phase instead of storing it.  seed may be NULL (all 1).
+ * No counterpart in the reference, whose followup maximises without
+ * gradients (simplex, MADS). */
+int pa_fstatnet_grad(pa_followup *fu, const double *sgnlo, int n, const double *seed, double *F,
+                     double *grad);
+
+/* Gradient ascent of F from n starting points sgnlo[n][4] (replaced by the
+ * final points), all points in lockstep on the device: quasi-Newton (BFGS)
+ * steps in scale units from the adjoint gradient, with a backtracking line
+ * search (a step is accepted when F grows by at least 1e-4 of the predicted
+ * gain, halved otherwise); the first step has length step0; a point stops
+ * when its step falls below min_step.  out[n][11] as pa_fstatnet() at the
+ * final points; iters[n] (may be NULL) the accepted steps.  No counterpart
+ * in the reference: it refines followup candidates beside the simplex
+ * (followup.c:1126-1174). */
+int pa_followup_ascent(pa_followup *fu, double *sgnlo, int n, const pa_ascent_opts *opts,
+                       double *out, int *iters);
+
+/* The reference simplex amoeba() (followup.c:971-1174) for n starting
+ * points at once, their F-statistic evaluations batched on the device:
+ * initial steps pc2[4], relative tolerance tol (the reference program uses
+ * 1e-7).  max_evals > 0 bounds the evaluations per point (the reference
+ * loops until the tolerance holds).  sgnlo[n][4] is replaced by the best
+ * vertex, out[n][11] is its fstat_out, nevals[n] (may be NULL) the
+ * evaluations made. */
+int pa_followup_simplex(pa_followup *fu, double *sgnlo, int n, const double *pc2, double tol,
+                        int max_evals, double *out, int *nevals);
+
+/* Device time of the last followup call (CUDA events on its stream), and
+ * the number of kernel launches so far. */
+double pa_followup_last_call_ms(const pa_followup *fu);
+long long pa_followup_kernel_launches(const pa_followup *fu);
+
 #ifdef __cplusplus
 }
 #endif

@@ -746,6 +746,7 @@ template <typename R, int PM> class EngineT : public Engine {
   Buffers b_;
   Geom gf_, gi_, gm_;
   long long launches_ = 0;
+  int split_ = 0;
 
   // CUDA events around a launch when profiling is on
   void pre(int kind, int items, cudaStream_t st) {
@@ -771,18 +772,21 @@ template <typename R, int PM> class EngineT : public Engine {
     }
   }
 
-  template <int SIGN, int LOGL, class Loader, class Storer>
+  // tw: W_L1 and W_L2 tables of the default split (L1 = 2^ceil(m/2)), then
+  // the two halves of the inter-pass twiddle; SPLIT 1 swaps the factors and
+  // so the first two tables.
+  template <int SIGN, int LOGL, int SPLIT, class Loader, class Storer>
   cudaError_t fft_l(const void* const* tw, const Loader& ld, const Storer& st, int batch, cudaStream_t stream,
                     int kind_a, int kind_b, void* ybuf) {
-    typedef FftShape<R, LOGL> G;
+    typedef FftShape<R, LOGL, SPLIT> G;
     constexpr int NT = TileCfg<R>::NT;
-    const T* t1 = (const T*)tw[0];
-    const T* t2 = (const T*)tw[1];
+    const T* t1 = (const T*)tw[SPLIT ? 1 : 0];
+    const T* t2 = (const T*)tw[SPLIT ? 0 : 1];
     const T* tlo = (const T*)tw[2];
     const T* thi = (const T*)tw[3];
     T* yb = (T*)ybuf;
-    auto ka = k_pass_a<R, SIGN, LOGL, Loader>;
-    auto kb = k_pass_b<R, SIGN, LOGL, Storer>;
+    auto ka = k_pass_a<R, SIGN, LOGL, Loader, SPLIT>;
+    auto kb = k_pass_b<R, SIGN, LOGL, Storer, SPLIT>;
     static bool doneA = false, doneB = false;
     smem_attr(ka, G::smem_a, doneA);
     smem_attr(kb, G::smem_b, doneB);
@@ -798,13 +802,17 @@ template <typename R, int PM> class EngineT : public Engine {
   }
 
   // Dispatch on the transform length (2^12 .. 2^20) to the compile-time
-  // geometry of the passes.
-  template <int SIGN, class Loader, class Storer>
+  // geometry of the passes; with SPLITS, odd lengths may take the swapped
+  // split (split = 1).
+  template <int SIGN, bool SPLITS = false, class Loader, class Storer>
   cudaError_t fft(const Geom& g, const void* const* tw, const Loader& ld, const Storer& st, int batch,
-                  cudaStream_t stream, int kind_a, int kind_b, void* ybuf) {
+                  cudaStream_t stream, int kind_a, int kind_b, void* ybuf, int split = 0) {
     switch (g.logL) {
-#define PA_FFT_CASE(M) \
-  case M: return fft_l<SIGN, M>(tw, ld, st, batch, stream, kind_a, kind_b, ybuf);
+#define PA_FFT_CASE(M)                                                                              \
+  case M:                                                                                           \
+    if (SPLITS && (M & 1) && split)                                                                 \
+      return fft_l<SIGN, M, SPLITS && (M & 1)>(tw, ld, st, batch, stream, kind_a, kind_b, ybuf);    \
+    return fft_l<SIGN, M, 0>(tw, ld, st, batch, stream, kind_a, kind_b, ybuf);
       PA_FFT_CASE(12) PA_FFT_CASE(13) PA_FFT_CASE(14) PA_FFT_CASE(15) PA_FFT_CASE(16)
       PA_FFT_CASE(17) PA_FFT_CASE(18) PA_FFT_CASE(19) PA_FFT_CASE(20)
 #undef PA_FFT_CASE
@@ -821,6 +829,8 @@ template <typename R, int PM> class EngineT : public Engine {
 
   long long launches() const override { return launches_; }
   size_t real_size() const override { return sizeof(R); }
+  void set_split(int split) override { split_ = (gm_.logL & 1) ? split : 0; }
+  int split() const override { return split_; }
 
   cudaError_t prelude(const SkyArgs& sky, int slot, cudaStream_t st) override {
     const int N = b_.N, nifo = b_.nifo;
@@ -881,7 +891,7 @@ template <typename R, int PM> class EngineT : public Engine {
     sl.M5 = sky.M5;
     sl.s1_0 = sky.s1_0;
     FstatStore<R> fs{(R*)b_.F, (const R*)b_.sums_r[slot], b_.nmin, b_.nmax, b_.bins};
-    cudaError_t e = fft<-1>(gm_, b_.tw_main, sl, fs, nb, st, KK_SPIN_A, KK_SPIN_B, b_.ybuf);
+    cudaError_t e = fft<-1, true>(gm_, b_.tw_main, sl, fs, nb, st, KK_SPIN_A, KK_SPIN_B, b_.ybuf, split_);
     if (e != cudaSuccess) return e;
     const int nchunk = (b_.bins + 4095) / 4096;
     pre(KK_THRESHOLD, nb, st);

@@ -117,6 +117,10 @@ class Engine {
                                 int s0_flag, cudaStream_t st, void* Fdbg) = 0;
   virtual long long launches() const = 0;
   virtual size_t real_size() const = 0;
+  // Factor split of the spindown FFT (0: L1 = 2^ceil(m/2); 1: swapped, for
+  // odd m only; ignored for even m).
+  virtual void set_split(int split) = 0;
+  virtual int split() const = 0;
 };
 
 // Factories (defined in the per-precision translation units).

@@ -253,10 +253,13 @@ template <typename R> __host__ __device__ constexpr int tile_pitch(int Cs) {
 }
 
 // Compile-time tile geometry of a length 2^LOGL transform.
-template <typename R, int LOGL> struct FftShape {
+// SPLIT 0: L1 = 2^ceil(m/2) (pass A has the longer columns); SPLIT 1 swaps
+// the two factors for odd m (pass A shorter columns, more per tile; the
+// radix schedules of the passes swap with them).
+template <typename R, int LOGL, int SPLIT = 0> struct FftShape {
   static constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
   static constexpr int logE = E == 8192 ? 13 : 12;
-  static constexpr int LOGL1 = (LOGL + 1) / 2, LOGL2 = LOGL / 2;
+  static constexpr int LOGL1 = SPLIT ? LOGL / 2 : (LOGL + 1) / 2, LOGL2 = LOGL - LOGL1;
   static constexpr int L1 = 1 << LOGL1, L2 = 1 << LOGL2;
   static constexpr int LOGC = logE - 1 - LOGL1, C = 1 << LOGC;      // pass-A columns per tile
   static constexpr int LOGRR = logE - 1 - LOGL2, RR = 1 << LOGRR;   // pass-B rows per tile
@@ -272,13 +275,13 @@ template <typename R, int LOGL> struct FftShape {
 // inter-pass twiddle W_L^{n2 k1} and writes Y[n2][k1][a|b] straight to
 // global memory, 16 contiguous bytes per lane.
 // Loader: prologue(batch, smem scratch) and load2(batch, n, a, b, scratch).
-template <typename R, int SIGN, int LOGL, class Loader>
+template <typename R, int SIGN, int LOGL, class Loader, int SPLIT = 0>
 __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
     k_pass_a(const Loader ld, const typename CT<R>::T* __restrict__ tw1,
              const typename CT<R>::T* __restrict__ twlo, const typename CT<R>::T* __restrict__ twhi,
              typename CT<R>::T* __restrict__ ybuf) {
   typedef typename CT<R>::T T;
-  typedef FftShape<R, LOGL> G;
+  typedef FftShape<R, LOGL, SPLIT> G;
   constexpr int E = G::E, NT = G::NT, P = G::PA;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s = reinterpret_cast<T*>(smem_raw);
@@ -318,12 +321,12 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
 // outputs X[k1 + L1 k2] for both arrays to the storer:
 //   __device__ void put(int batch, int k1, int k2, T a, T b, int logL1) const
 // with consecutive lanes on consecutive k1.
-template <typename R, int SIGN, int LOGL, class Storer>
+template <typename R, int SIGN, int LOGL, class Storer, int SPLIT = 0>
 __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
     k_pass_b(const Storer st, const typename CT<R>::T* __restrict__ tw2,
              const typename CT<R>::T* __restrict__ ybuf) {
   typedef typename CT<R>::T T;
-  typedef FftShape<R, LOGL> G;
+  typedef FftShape<R, LOGL, SPLIT> G;
   constexpr int E = G::E, NT = G::NT, P = G::PB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s = reinterpret_cast<T*>(smem_raw);

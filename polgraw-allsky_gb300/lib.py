@@ -30,6 +30,8 @@ EXPORTS = [
     "pa_host_create", "pa_host_setup", "pa_host_search", "pa_host_main", "pa_host_destroy",
     "pa_host_settings", "pa_host_detectors", "pa_host_range", "pa_host_core_opts",
     "pa_host_config", "pa_host_detector_name",
+    "pa_followup_create", "pa_followup_destroy", "pa_followup_last_error", "pa_fstatnet", "pa_fstatnet_grad",
+    "pa_followup_ascent", "pa_followup_simplex", "pa_followup_last_call_ms", "pa_followup_kernel_launches",
 ]
 
 
@@ -109,6 +111,23 @@ def load(path: str | None = None) -> C.CDLL:
                                    P(C.c_longlong)]
     lib.pa_fstat_noalloc.argtypes = [P(Settings), P(Detector), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                      P(Opts), C.c_int, P(C.c_double)]
+    lib.pa_followup_create.restype = C.c_void_p
+    lib.pa_followup_create.argtypes = [P(Settings), P(Detector), C.c_int, P(Config), P(C.c_int)]
+    lib.pa_followup_destroy.argtypes = [C.c_void_p]
+    lib.pa_followup_destroy.restype = None
+    lib.pa_followup_last_error.restype = C.c_char_p
+    lib.pa_followup_last_error.argtypes = [C.c_void_p]
+    lib.pa_fstatnet.argtypes = [C.c_void_p, P(C.c_double), C.c_int, P(C.c_double)]
+    lib.pa_fstatnet_grad.argtypes = [C.c_void_p, P(C.c_double), C.c_int, P(C.c_double), P(C.c_double),
+                                     P(C.c_double)]
+    lib.pa_followup_ascent.argtypes = [C.c_void_p, P(C.c_double), C.c_int, P(AscentOpts), P(C.c_double),
+                                       P(C.c_int)]
+    lib.pa_followup_simplex.argtypes = [C.c_void_p, P(C.c_double), C.c_int, P(C.c_double), C.c_double, C.c_int,
+                                        P(C.c_double), P(C.c_int)]
+    lib.pa_followup_last_call_ms.restype = C.c_double
+    lib.pa_followup_last_call_ms.argtypes = [C.c_void_p]
+    lib.pa_followup_kernel_launches.restype = C.c_longlong
+    lib.pa_followup_kernel_launches.argtypes = [C.c_void_p]
     lib.pa_host_create.restype = C.c_void_p
     lib.pa_host_create.argtypes = [C.c_int, P(C.c_char_p), P(C.c_int)]
     lib.pa_host_setup.argtypes = [C.c_void_p]
@@ -323,6 +342,94 @@ class Context:
         if self.ctx:
             self.lib.pa_destroy(self.ctx)
             self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class AscentOpts(C.Structure):
+    _fields_ = [("scale", C.c_double * 4), ("step0", C.c_double), ("min_step", C.c_double), ("max_iter", C.c_int)]
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Followup:
+    """pa_followup: the demodulated network F-statistic (followup.c
+    Fstatnet), its adjoint gradient, gradient ascent and the batched
+    reference simplex.  Points are rows (f, s, delta, alpha)."""
+
+    def __init__(self, settings: Settings, dets, nifo: int, precision: int = PA_PREC_MIXED, device: int = 0):
+        self.lib = load()
+        cfg = Config(precision, PA_PHASE_F64, 0, device)
+        st = C.c_int(0)
+        self.fu = self.lib.pa_followup_create(C.byref(settings), dets, nifo, C.byref(cfg), C.byref(st))
+        if not self.fu:
+            raise SearchError("pa_followup_create failed (%d): %s" %
+                              (st.value, self.lib.pa_followup_last_error(None).decode()))
+
+    def _check(self, rc, what):
+        if rc != PA_OK:
+            raise SearchError("%s failed (%d): %s" % (what, rc, self.lib.pa_followup_last_error(self.fu).decode()))
+
+    @staticmethod
+    def _pts(sgnlo) -> np.ndarray:
+        return np.ascontiguousarray(np.atleast_2d(np.asarray(sgnlo, dtype=np.float64)))
+
+    def fstatnet(self, sgnlo) -> np.ndarray:
+        """fstat_out rows [n, 11] (out[:, 5] = -F)."""
+        p = self._pts(sgnlo)
+        out = np.zeros((len(p), 11))
+        self._check(self.lib.pa_fstatnet(self.fu, _dp(p), len(p), _dp(out)), "pa_fstatnet")
+        return out
+
+    def fstatnet_grad(self, sgnlo, seed=None):
+        """(F [n], grad [n, 4]) with grad = seed * dF/d(f, s, delta, alpha)."""
+        p = self._pts(sgnlo)
+        n = len(p)
+        F = np.zeros(n)
+        g = np.zeros((n, 4))
+        sd = None if seed is None else np.ascontiguousarray(seed, dtype=np.float64)
+        self._check(self.lib.pa_fstatnet_grad(self.fu, _dp(p), n, None if sd is None else _dp(sd), _dp(F), _dp(g)),
+                    "pa_fstatnet_grad")
+        return F, g
+
+    def ascent(self, sgnlo, scale, step0: float = 0.25, min_step: float = 1e-3, max_iter: int = 100):
+        """Gradient ascent; returns (points [n, 4], fstat_out [n, 11], iters [n])."""
+        p = self._pts(sgnlo).copy()
+        n = len(p)
+        out = np.zeros((n, 11))
+        it = np.zeros(n, dtype=np.int32)
+        o = AscentOpts((C.c_double * 4)(*[float(x) for x in scale]), step0, min_step, max_iter)
+        self._check(self.lib.pa_followup_ascent(self.fu, _dp(p), n, C.byref(o), _dp(out),
+                                                it.ctypes.data_as(C.POINTER(C.c_int))), "pa_followup_ascent")
+        return p, out, it
+
+    def simplex(self, sgnlo, pc2, tol: float = 1e-7, max_evals: int = 0):
+        """The reference simplex; returns (points [n, 4], fstat_out [n, 11], nevals [n])."""
+        p = self._pts(sgnlo).copy()
+        n = len(p)
+        out = np.zeros((n, 11))
+        nev = np.zeros(n, dtype=np.int32)
+        st = np.ascontiguousarray(pc2, dtype=np.float64)
+        self._check(self.lib.pa_followup_simplex(self.fu, _dp(p), n, _dp(st), tol, max_evals, _dp(out),
+                                                 nev.ctypes.data_as(C.POINTER(C.c_int))), "pa_followup_simplex")
+        return p, out, nev
+
+    def last_call_ms(self) -> float:
+        return self.lib.pa_followup_last_call_ms(self.fu)
+
+    def launches(self) -> int:
+        return self.lib.pa_followup_kernel_launches(self.fu)
+
+    def close(self):
+        if getattr(self, "fu", None):
+            self.lib.pa_followup_destroy(self.fu)
+            self.fu = None
 
     def __del__(self):
         try:

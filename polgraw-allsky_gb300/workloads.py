@@ -80,3 +80,50 @@ def nearest_sky(host, inj):
     a = np.array([[s.M[10], s.M[14]], [s.M[11], s.M[15]]])
     nn, mm = np.linalg.solve(a, np.array(be) * s.oms)
     return (pm, int(round(mm)), int(round(nn)))
+
+
+def peak_widths(settings, dets, nifo, delta, alpha):
+    """Widths of the demodulated F-statistic peak in (f, s, delta, alpha):
+    2 pi/N, 2 pi/N^2, and for each sky angle the step that turns the phase
+    by 2 pi across the data, 2 pi / (oms * spread of d shft/d angle)."""
+    N = settings.N
+    sd, cd, sa, ca = np.sin(delta), np.cos(delta), np.sin(alpha), np.cos(alpha)
+    spread_d, spread_a = 0.0, 0.0
+    for n in range(nifo):
+        R = np.ctypeslib.as_array(dets[n].DetSSB, shape=(3 * N,)).reshape(N, 3)
+        dd = R @ np.array([-ca * sd, -sa * sd, cd])
+        da = R @ np.array([-sa * cd, ca * cd, 0.0])
+        spread_d = max(spread_d, float(dd.max() - dd.min()))
+        spread_a = max(spread_a, float(da.max() - da.min()))
+    oms = settings.oms
+    return [2 * np.pi / N, 2 * np.pi / float(N) ** 2, 2 * np.pi / (oms * spread_d), 2 * np.pi / (oms * spread_a)]
+
+
+def followup(root: str):
+    """The followup workload: H1+L1+V1, N=86164 (2 sidereal days at dt=2 s),
+    4 injected signals (SNR 10-15, seed 2005).  Returns (command line,
+    injections); candidates_around() makes the starting points."""
+    ds = synth.write_dataset(root, ident=1, band=666, dt=2.0, nod=2, fftpad=1, dets=["H1", "L1", "V1"],
+                             M=None)
+    inj = _inject_random(ds, np.random.default_rng(2005), 4, fdot_lo=-1e-8, fdot_hi=1e-8,
+                         snr_lo=10, snr_hi=15)
+    return ["-data", root, "-ident", "1", "-band", "666", "-dt", "2", "-nod", "2",
+            "-output", os.path.join(root, "out"), "--nocheckpoint"], inj
+
+
+def candidates_around(host, inj, n: int, seed: int = 2005):
+    """n starting points spread over the injections, each offset from its
+    injection by U(-0.5, 0.5) peak widths in every parameter; returns
+    (points [n, 4], widths [n, 4], index of the injection per point)."""
+    dets, nifo = host.detectors()
+    rng = np.random.default_rng(seed)
+    pts, ws, which = [], [], []
+    for k in range(n):
+        j = k % len(inj)
+        c = inj[j]
+        w = peak_widths(host.settings, dets, nifo, c["delta"], c["alpha"])
+        base = [c["f"], c["fdot"], c["delta"], c["alpha"]]
+        pts.append([base[t] + float(rng.uniform(-0.5, 0.5)) * w[t] for t in range(4)])
+        ws.append(w)
+        which.append(j)
+    return np.array(pts), np.array(ws), np.array(which)

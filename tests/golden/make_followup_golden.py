@@ -52,18 +52,8 @@ from casegen import materialize  # noqa: E402
 
 
 def peak_widths(settings, dets, nifo, delta, alpha):
-    """(f, s, delta, alpha) widths of the F-statistic peak (see module doc)."""
-    N = settings.N
-    sd, cd, sa, ca = np.sin(delta), np.cos(delta), np.sin(alpha), np.cos(alpha)
-    spread_d, spread_a = 0.0, 0.0
-    for n in range(nifo):
-        R = np.ctypeslib.as_array(dets[n].DetSSB, shape=(3 * N,)).reshape(N, 3)
-        dd = R @ np.array([-ca * sd, -sa * sd, cd])
-        da = R @ np.array([-sa * cd, ca * cd, 0.0])
-        spread_d = max(spread_d, float(dd.max() - dd.min()))
-        spread_a = max(spread_a, float(da.max() - da.min()))
-    oms = settings.oms
-    return [2 * np.pi / N, 2 * np.pi / float(N) ** 2, 2 * np.pi / (oms * spread_d), 2 * np.pi / (oms * spread_a)]
+    from polgraw_gb300 import workloads
+    return workloads.peak_widths(settings, dets, nifo, delta, alpha)
 
 
 def followup_points(case, settings, dets, nifo, seed=2005, n=16):
@@ -108,7 +98,8 @@ def run_case(case: dict) -> dict:
             nev = lib.ref_fu_amoeba(pt.ctypes.data_as(P), pc2.ctypes.data_as(P), 1e-7, out.ctypes.data_as(P))
             am.append({"start": start.tolist(), "pc2": pc2.tolist(), "tol": 1e-7, "point": pt.tolist(),
                        "out": out.tolist(), "nevals": int(nev)})
-        return {"case": case["name"], "inputs": m["ds"].files, "args": m["args"], "N": s.N, "nifo": nifo,
+        args = [a.replace(data, "<data>") for a in m["args"]]
+        return {"case": case["name"], "inputs": m["ds"].files, "args": args, "N": s.N, "nifo": nifo,
                 "widths": w, "points": pts, "fstatnet": fst, "amoeba": am,
                 "generator": "followup/src/followup.c evaluate_simplex(dim=0) and amoeba(), "
                              "built by oracle/build_oracle.py"}

@@ -1,0 +1,193 @@
+"""Followup on the GPU: the demodulated network F-statistic (pa_fstatnet),
+its adjoint gradient (pa_fstatnet_grad), gradient ascent and the batched
+reference simplex, checked against the reference followup program's own
+outputs (tests/golden/fu_h1l1v1.json, made from followup/src/followup.c) and
+the FP64 oracle gradient.
+
+Tolerances: F within 1e-4 relative (mixed: FP32 data, FP64 phase) and 1e-10
+(FP64 form); gradients compared in peak-width units, w_j dF/dtheta_j, to
+2e-3 (mixed) and 1e-8 (FP64) of the largest component at the point.
+"""
+import numpy as np
+import pytest
+
+from casegen import materialize
+from cases import FOLLOWUP_CASES
+from helpers import golden
+
+pytestmark = pytest.mark.gpu
+
+FORMS = {"mixed": (0, 1e-4, 2e-3), "fp64": (1, 1e-10, 1e-8)}
+
+
+@pytest.fixture(scope="module")
+def fu_case(tmp_path_factory):
+    from polgraw_gb300.lib import Host
+    from pyoracle import FollowupOracle
+    case = FOLLOWUP_CASES[0]
+    g = golden(case["name"])
+    tmp = tmp_path_factory.mktemp("fu")
+    data = tmp / "data"
+    data.mkdir()
+    m = materialize(case, str(data))
+    assert m["ds"].files == g["inputs"], "synthetic inputs differ from the golden run's"
+    host = Host(m["args"] + ["-output", str(tmp / "out"), "--nocheckpoint"])
+    dets, nifo = host.detectors()
+    return host, dets, nifo, g, FollowupOracle(host.settings, dets, nifo)
+
+
+def _fu(fu_case, form):
+    from polgraw_gb300.lib import Followup
+    host, dets, nifo, g, _ = fu_case
+    return Followup(host.settings, dets, nifo, precision=FORMS[form][0])
+
+
+@pytest.mark.parametrize("form", list(FORMS))
+def test_fstatnet_matches_reference(form, fu_case, gpu_ok):
+    g = fu_case[3]
+    fu = _fu(fu_case, form)
+    out = fu.fstatnet(g["points"])
+    ref = np.array(g["fstatnet"])
+    tol = FORMS[form][1]
+    F, Fr = -out[:, 5], -ref[:, 5]
+    assert np.abs(F - Fr).max() / Fr.max() < tol, np.abs(F - Fr) / Fr.max()
+    # amplitude estimates and SNRs, relative to their scale at each point
+    amp = np.abs(ref[:, :4]).max(axis=1, keepdims=True)
+    assert np.abs(out[:, :4] - ref[:, :4]).max() <= 10 * tol * amp.max()
+    assert np.allclose(out[:, 6:10], ref[:, 6:10], rtol=0, atol=0)
+    assert np.abs(out[:, 10] - ref[:, 10]).max() / ref[:, 10].max() < 10 * tol
+
+
+@pytest.mark.parametrize("form", list(FORMS))
+def test_batch_independent(form, fu_case, gpu_ok):
+    g = fu_case[3]
+    fu = _fu(fu_case, form)
+    pts = np.array(g["points"])
+    whole = fu.fstatnet(pts)
+    for k in (0, 5, len(pts) - 1):
+        one = fu.fstatnet(pts[k:k + 1])
+        assert np.array_equal(one[0], whole[k])
+
+
+@pytest.mark.parametrize("form", list(FORMS))
+def test_adjoint_gradient_matches_fp64_oracle(form, fu_case, gpu_ok):
+    g, ora = fu_case[3], fu_case[4]
+    fu = _fu(fu_case, form)
+    w = np.array(g["widths"])
+    pts = np.array(g["points"])
+    F, grad = fu.fstatnet_grad(pts)
+    out = fu.fstatnet(pts)
+    assert np.allclose(F, -out[:, 5], rtol=1e-12, atol=0)
+    tol = FORMS[form][2]
+    for k, p in enumerate(pts):
+        Fo, go = ora.fstatnet_grad(p)
+        scale = np.abs(w * go).max()
+        err = np.abs(w * (grad[k] - go)).max()
+        assert err <= tol * scale, (k, w * grad[k], w * go)
+    # seeds scale the gradient
+    seed = np.linspace(0.5, 2.0, len(pts))
+    _, gs = fu.fstatnet_grad(pts, seed=seed)
+    want = w * grad * seed[:, None]
+    rel = np.abs(w * gs - want).max(axis=1) / np.abs(want).max(axis=1)
+    assert rel.max() <= (1e-4 if form == "mixed" else 1e-12), rel
+
+
+def test_adjoint_matches_finite_differences_fp64(fu_case, gpu_ok):
+    """Central differences of the GPU's own FP64 F against its adjoint."""
+    g = fu_case[3]
+    fu = _fu(fu_case, "fp64")
+    w = np.array(g["widths"])
+    for p in np.array(g["points"])[1:5]:
+        F, grad = fu.fstatnet_grad(p)
+        fd = np.zeros(4)
+        for j in range(4):
+            h = np.zeros(4)
+            h[j] = 1e-4 * w[j]
+            o = fu.fstatnet(np.stack([p + h, p - h]))
+            fd[j] = (-o[0, 5] + o[1, 5]) / (2 * h[j])
+        scale = np.abs(w * grad[0]).max()
+        assert np.abs(w * (grad[0] - fd)).max() <= 1e-5 * scale
+
+
+def test_autograd_function(fu_case, gpu_ok):
+    """The adjoint behind a torch.autograd.Function (test harness only): the
+    backward pass returns grad_output * dF/dtheta, the directional derivative
+    matches a central difference, and an optimiser step in peak-width units
+    raises F."""
+    torch = pytest.importorskip("torch")
+    g = fu_case[3]
+    fu = _fu(fu_case, "mixed")
+    w = torch.tensor(g["widths"], dtype=torch.float64)
+
+    class Fstat(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, theta):
+            F, grad = fu.fstatnet_grad(theta.detach().cpu().numpy())
+            ctx.save_for_backward(torch.from_numpy(grad))
+            return torch.from_numpy(F)
+
+        @staticmethod
+        def backward(ctx, gout):
+            (grad,) = ctx.saved_tensors
+            return gout[:, None] * grad
+
+    pts = torch.tensor(g["points"][1:9], dtype=torch.float64)
+    u = (pts / w).clone().requires_grad_(True)   # peak-width units
+    F0 = Fstat.apply(u * w)
+    F0.sum().backward()
+    _, grad = fu.fstatnet_grad(pts.numpy())
+    assert torch.allclose(u.grad, torch.from_numpy(grad) * w, rtol=1e-12, atol=0)
+    # the directional derivative along the gradient matches a central
+    # difference of F (curvature cancels; tolerance covers the FP32 noise of F)
+    d = u.grad / u.grad.norm(dim=1, keepdim=True)
+    h = 1e-3
+    with torch.no_grad():
+        Fp = Fstat.apply((u + h * d) * w)
+        Fm = Fstat.apply((u - h * d) * w)
+    fd = (Fp - Fm) / (2 * h)
+    slope = (u.grad * d).sum(dim=1)
+    assert torch.allclose(fd, slope, rtol=2e-2, atol=0), (fd, slope)
+    # one optimiser step of 0.01 peak widths along the normalised gradient
+    # raises the summed F
+    u.grad = d.clone()
+    opt = torch.optim.SGD([u], lr=1e-2, maximize=True)
+    opt.step()
+    with torch.no_grad():
+        F1 = Fstat.apply(u * w)
+    assert float(F1.sum()) > float(F0.detach().sum())
+
+
+@pytest.mark.parametrize("form", list(FORMS))
+def test_simplex_matches_reference(form, fu_case, gpu_ok):
+    g = fu_case[3]
+    fu = _fu(fu_case, form)
+    am = g["amoeba"]
+    starts = np.array([a["start"] for a in am])
+    pts, out, nev = fu.simplex(starts, am[0]["pc2"], tol=am[0]["tol"], max_evals=5000)
+    w = np.array(g["widths"])
+    for k, a in enumerate(am):
+        Fr = -a["out"][5]
+        # same maximum: F within the tolerance, point within 0.05 widths
+        assert -out[k, 5] >= Fr * (1 - 10 * FORMS[form][1]), (k, -out[k, 5], Fr)
+        assert np.abs((pts[k] - np.array(a["point"])) / w).max() < 0.05
+        if form == "fp64":
+            assert abs(int(nev[k]) - a["nevals"]) <= 0.2 * a["nevals"]
+    # the batch of three and each start alone give the same result
+    p1, o1, n1 = fu.simplex(starts[1:2], am[0]["pc2"], tol=am[0]["tol"], max_evals=5000)
+    assert np.array_equal(p1[0], pts[1]) and n1[0] == nev[1]
+
+
+@pytest.mark.parametrize("form", list(FORMS))
+def test_ascent_reaches_simplex_maximum(form, fu_case, gpu_ok):
+    g = fu_case[3]
+    fu = _fu(fu_case, form)
+    w = np.array(g["widths"])
+    starts = np.array(g["points"][1:])
+    F0 = -fu.fstatnet(starts)[:, 5]
+    pts, out, it = fu.ascent(starts, w, step0=0.25, min_step=1e-4, max_iter=200)
+    F1 = -out[:, 5]
+    assert np.all(F1 >= F0)
+    Fmax = max(-a["out"][5] for a in g["amoeba"])
+    # every start lies within 0.5 widths of the injection: all reach its peak
+    assert np.all(F1 >= Fmax * (1 - 1e-3)), (F1, Fmax)
+    assert np.all(it > 0)
