@@ -311,6 +311,82 @@ def run_followup(args, L):
     print(json.dumps(line))
 
 
+def run_segments(args, L):
+    """Multi-segment workload: segments of uneven N (uniform in [60000,
+    260000], seed 2004), H1+L1, fftpad=2, 300 sky x 150 spindowns each.
+    Timed three ways on the same contexts: one segment after another
+    (pa_search_batch each, default schedule); all segments at once on their
+    own streams (pa_segments_search, default schedule, no graph); and all
+    at once as one CUDA graph after pa_autotune of every segment."""
+    segs = workloads.segments(args.segments, nsky=300, nspin=150)
+    ctxs = [L.Context(g["settings"], g["dets"], 2, precision=L.PA_PREC_MIXED, phase_mode=L.PA_PHASE_FIXED)
+            for g in segs]
+    nspin = 150
+    templates = sum(len(g["tasks"]) * nspin * (g["settings"].nmax - g["settings"].nmin) for g in segs)
+    tl = [g["tasks"] for g in segs]
+    ol = [g["opts"] for g in segs]
+    rl = [g["range"] for g in segs]
+
+    def serial():
+        ms = 0.0
+        for c, g in zip(ctxs, segs):
+            c.search_batch(g["tasks"], g["opts"], g["range"])
+            ms += c.last_call_ms()
+        return ms
+
+    for _ in range(args.warmup):
+        serial()
+    t_serial = 0.0
+    for _ in range(args.steps):
+        l2_flush()
+        t_serial += serial()
+    seg = L.Segments(ctxs, graph=False)
+    for _ in range(args.warmup):
+        seg.search(tl, ol, rl)
+    t_fixed = 0.0
+    for _ in range(args.steps):
+        l2_flush()
+        res_fixed = seg.search(tl, ol, rl)
+        t_fixed += seg.last_call_ms()
+    t0 = time.perf_counter()
+    sched = [c.autotune(g["tasks"][:4], g["opts"], g["range"]) for c, g in zip(ctxs, segs)]
+    t_tune = time.perf_counter() - t0
+    seg.set_graph(True)
+    for _ in range(args.warmup):
+        seg.search(tl, ol, rl)
+    launches0 = sum(c.launches() for c in ctxs)
+    clocks = ClockSampler(0)
+    t_tuned = 0.0
+    for _ in range(args.steps):
+        l2_flush()
+        res_tuned = seg.search(tl, ol, rl)
+        t_tuned += seg.last_call_ms()
+    clk = clocks.stop()
+    launches = (sum(c.launches() for c in ctxs) - launches0) // max(1, args.steps)
+    # the schedules may differ in FFT rounding only: same candidate indices
+    same = all(sorted(map(tuple, r1[1][["pm", "mm", "nn", "ss", "ii"]].tolist())) ==
+               sorted(map(tuple, r2[1][["pm", "mm", "nn", "ss", "ii"]].tolist()))
+               for r1, r2 in zip(res_fixed, res_tuned))
+    value = templates * args.steps / (t_tuned / 1e3)
+    Ns = [g["N"] for g in segs]
+    line = {"metric": "templates/sec (sky x spindown x bin), multi-segment batch",
+            "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_tuned / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64phase", "data": "synthetic",
+            "config": {"workload": "%d segments, N uniform in [60000, 260000] (seed 2004), dt=2s, H1+L1, fftpad=2, "
+                                   "300 sky x 150 spindowns per segment" % len(segs),
+                       "N_min": min(Ns), "N_max": max(Ns), "nfftf": sorted({g["settings"].nfftf for g in segs}),
+                       "l2": "flushed (256 MB write) before each timed step"},
+            "clocks": clk, "gpu_launches": int(launches),
+            "serial_templates_per_s": templates * args.steps / (t_serial / 1e3),
+            "fixed_schedule_templates_per_s": templates * args.steps / (t_fixed / 1e3),
+            "tuned_graph_templates_per_s": value,
+            "autotune": {"seconds": t_tune, "schedules": [list(x) for x in sched]},
+            "candidates_identical_fixed_vs_tuned": bool(same)}
+    seg.close()
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -323,10 +399,14 @@ def main():
     ap.add_argument("--fp64-sky", type=int, default=48, help="sky points timed in the all-FP64 form")
     ap.add_argument("--cpu-sky", type=int, default=48, help="sky points in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--workload", default="network", choices=["network", "stress", "followup"],
+    ap.add_argument("--segments", type=int, default=24, help="segments workload: number of segments")
+    ap.add_argument("--workload", default="network", choices=["network", "stress", "followup", "segments"],
                     help="stress: the N=258492 precision-stress workload, every precision form; "
                          "followup: demodulated F-statistic, adjoint, ascent and simplex on 4096 candidates")
     ap.add_argument("--candidates", type=int, default=4096, help="followup workload: candidates")
+    ap.add_argument("--graphs", type=int, default=1, help="capture each batch into a CUDA graph (1) or not (0)")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="tune the spindown schedule (pa_autotune) on 8 sky points before timing (1) or not (0)")
     ap.add_argument("--cpu-candidates", type=int, default=4, help="followup: CPU simplex sample")
     args = ap.parse_args()
 
@@ -342,6 +422,10 @@ def main():
         if rank == 0:
             run_followup(args, L)
         return
+    if args.workload == "segments":
+        if rank == 0:
+            run_segments(args, L)
+        return
     tmp = tempfile.mkdtemp(prefix="pa_bench_")
     argv = make_workload(tmp, args.spindowns)
     host = L.Host(argv)
@@ -350,6 +434,7 @@ def main():
     bins = s.nmax - s.nmin
     nspin = args.spindowns
     cfg = {"workload": WORKLOAD, "sky_points": len(tasks), "spindowns": nspin, "bins": bins,
+           "graphs": bool(args.graphs),
            "nifo": 2, "N": s.N, "nfftf": s.nfftf, "phase": args.phase,
            "l2": "flushed (256 MB write) before each timed step", "parallelism": "replicas" if world > 1 else "1 GPU"}
 
@@ -386,6 +471,10 @@ def main():
     ctx = L.Context(s, dets, nifo, precision=L.PA_PREC_MIXED, phase_mode=phase, device=0)
     opts, rng = host.opts(), host.range
     templates = len(tasks) * nspin * bins
+    if args.autotune:
+        ctx.autotune(tasks[:8], opts, rng)
+    ctx.set_graphs(bool(args.graphs))
+    sched = ctx.schedule()
     for _ in range(args.warmup):
         ctx.search_batch(tasks, opts, rng)
     launches0 = ctx.launches()
@@ -419,7 +508,8 @@ def main():
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64phase", "data": "synthetic", "config": cfg,
            "clocks": clk, "gpu_launches": int(launches),
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-           "candidates_per_step": ncand}
+           "candidates_per_step": ncand,
+           "schedule": {"spindown_batch": sched[0], "fft_split": sched[1], "autotuned": bool(args.autotune)}}
 
     if not args.no_extras:
         # per-kernel CUDA-event profile of one step (not the timed number)

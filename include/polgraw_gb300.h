@@ -220,6 +220,71 @@ int pa_profile_get(const pa_ctx *ctx, int kind, const char **name, double *total
                    long long *launches, long long *items);
 
 /* ------------------------------------------------------------------------
+ * Launch schedule, CUDA graphs and the multi-segment front-end.  No
+ * counterpart in the reference (one process per segment and sky range,
+ * search/network/src-cpu/jobcore.c:51-184).
+ * ------------------------------------------------------------------------ */
+
+/* CUDA graphs on/off (default off): when on, each pa_search_batch /
+ * pa_job_core call captures its launches (both streams) into a CUDA graph,
+ * updated in place when the next call has the same launch structure, and
+ * launches it once.  Results are identical either way. */
+int pa_set_graphs(pa_ctx *ctx, int on);
+
+/* Spindown-loop schedule: spindowns per fused launch (1 .. *max_sbatch, the
+ * batch the buffers were sized for, twice the automatic default) and the
+ * factor split of the spindown FFT (0: L1 = 2^ceil(m/2), the default; 1:
+ * swapped factors, different radix schedule of the two passes; for odd
+ * m = log2(nfftf) only, ignored otherwise). */
+int pa_set_schedule(pa_ctx *ctx, int sbatch, int split);
+int pa_get_schedule(const pa_ctx *ctx, int *sbatch, int *split, int *max_sbatch);
+
+/* Times the candidate schedules (three spindown batches x the possible
+ * splits) on the given sky points (each searched three times, the first as
+ * warm-up, CUDA-event device time) and keeps the fastest; returns it in
+ * *sbatch, *split (either may be NULL).  Results do not depend on sbatch;
+ * the split changes FFT rounding only. */
+int pa_autotune(pa_ctx *ctx, const pa_sky *tasks, int ntasks, const pa_opts *opts, const pa_range *s_range,
+                int *sbatch, int *split);
+
+/* Several data segments searched together: one context per segment (own
+ * N, FFT lengths, data), their batches enqueued at once on their own
+ * streams, forked from one origin stream, so that the GPU runs them
+ * concurrently; with the graph on (default) the whole multi-segment
+ * workload is captured into one CUDA graph (updated in place on the next
+ * call with the same launch structure) and launched once. */
+typedef struct pa_segments pa_segments;
+
+/* One segment's batch: the arguments of pa_search_batch() for context k. */
+typedef struct pa_segment_job {
+  const pa_sky *tasks;
+  int ntasks;
+  const pa_opts *opts;
+  const pa_range *range;
+  int *sgnlc;
+  double *sgnlv;
+  int cap;
+  pa_cand_idx *idx;
+  int *FNum;
+  int *needed;
+} pa_segment_job;
+
+/* The contexts stay owned by the caller and must outlive the handle; all on
+ * one device. */
+pa_segments *pa_segments_create(pa_ctx *const *ctxs, int nseg, int *status);
+void pa_segments_destroy(pa_segments *seg);
+const char *pa_segments_last_error(const pa_segments *seg);
+int pa_segments_set_graph(pa_segments *seg, int on);
+/* jobs[k] runs on context k; status[k] (may be NULL) receives each
+ * segment's result as pa_search_batch() would return it; the return value
+ * is the first non-OK status.  Records are appended per segment exactly as
+ * pa_search_batch() on that context would append them. */
+int pa_segments_search(pa_segments *seg, const pa_segment_job *jobs, int *status);
+/* Device time of the last pa_segments_search (CUDA events on the origin
+ * stream around all segments). */
+double pa_segments_last_call_ms(const pa_segments *seg);
+
+/* ------------------------------------------------------------------------
  * Followup: the demodulated network F-statistic of followup/src/followup.c
  * at arbitrary (f, s, delta, alpha), its adjoint gradient, and maximisers.
  * A point is sgnlo = (f [rad/sample], s [rad/sample^2], delta, alpha [rad])

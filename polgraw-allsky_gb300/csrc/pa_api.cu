@@ -56,6 +56,12 @@ struct pa_ctx {
   pa::Prof prof;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.;
+  // CUDA graph of a batch (captured launches, updated in place when the next
+  // batch has the same launch structure)
+  bool graphs = false;
+  cudaGraphExec_t gexec = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int sb_max = 0;  // spindown batch the buffers are sized for
 };
 
 namespace pa {
@@ -245,6 +251,9 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
     sb = (int)std::max<size_t>(1, std::min<size_t>(64, ((size_t)64 << 20) / per));
   }
   b.sbatch = sb;
+  // buffers for up to twice the batch, for the schedule tuner
+  c->sb_max = std::min(128, 2 * sb);
+  const int sbm = c->sb_max;
   const size_t rs = c->rsz, cs = 2 * c->rsz;
   int rc;
 #define ALLOC(ptr, bytes)                              \
@@ -276,9 +285,9 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   ALLOC(b.ybuf_pre, cs * nifo * 2 * (size_t)s.Ninterp);
   ALLOC(b.counter, sizeof(unsigned int) * 4);
   CK(cudaMemset(b.counter, 0, sizeof(unsigned int) * 4), "cudaMemset");
-  ALLOC(b.ybuf, (size_t)sb * 2 * s.nfftf * cs);
-  ALLOC(b.F, rs * (size_t)sb * b.bins);
-  ALLOC(b.mu, rs * (size_t)sb * (b.nblk > 0 ? b.nblk : 1));
+  ALLOC(b.ybuf, (size_t)sbm * 2 * s.nfftf * cs);
+  ALLOC(b.F, rs * (size_t)sbm * b.bins);
+  ALLOC(b.mu, rs * (size_t)sbm * (b.nblk > 0 ? b.nblk : 1));
   b.cand_cap = 1 << 18;
   ALLOC(b.cand, sizeof(pa::DevCand) * (size_t)b.cand_cap);
   ALLOC(b.ncand, sizeof(int) * 4);
@@ -317,6 +326,8 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   c->eng->prof = &c->prof;
   CK(cudaEventCreate(&c->ev0), "cudaEventCreate");
   CK(cudaEventCreate(&c->ev1), "cudaEventCreate");
+  CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+  CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "cudaEventCreate");
   return PA_OK;
 }
 
@@ -405,6 +416,9 @@ void pa_destroy(pa_ctx* c) {
   delete[] c->prof.recs;
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
   for (void* p : c->allocs) cudaFree(p);
   if (c->h_cand) cudaFreeHost(c->h_cand);
   if (c->h_ncand) cudaFreeHost(c->h_ncand);
@@ -555,10 +569,11 @@ pa::SkyArgs sky_args(const pa_ctx* c, const SkyHost& h, int task) {
 // Enqueues one sky point: its prelude on the prelude stream into slot
 // task % 2 (after the spindowns that last read that slot), and its spindown
 // batches on the main stream (after the prelude).
-int enqueue_sky(pa_ctx* c, const SkyHost& h, const pa_opts* o, int task, void* Fdbg, int Fss) {
+int enqueue_sky(pa_ctx* c, const SkyHost& h, const pa_opts* o, int task, void* Fdbg, int Fss,
+                bool wait_slot = true) {
   const pa::SkyArgs a = sky_args(c, h, task);
   const int slot = task & 1;
-  CK(cudaStreamWaitEvent(c->stream_pre, c->ev_spin[slot], 0), "cudaStreamWaitEvent");
+  if (wait_slot) CK(cudaStreamWaitEvent(c->stream_pre, c->ev_spin[slot], 0), "cudaStreamWaitEvent");
   cudaError_t e = c->eng->prelude(a, slot, c->stream_pre);
   if (e != cudaSuccess) return cuda_fail(c, e, "prelude launch");
   CK(cudaEventRecord(c->ev_pre[slot], c->stream_pre), "cudaEventRecord");
@@ -583,6 +598,115 @@ bool cand_less(const pa::DevCand& x, const pa::DevCand& y) {
   return x.ii < y.ii;
 }
 
+// Enqueues a batch on the context's streams: the candidate counter reset,
+// then every sky point (prelude on the prelude stream forked from the main
+// stream, spindowns on the main stream), and the join of the prelude stream
+// back into the main stream.  Slots are reused across sky points through
+// their events; the first use of each slot in a batch needs no wait (the
+// previous batch finished before this call).  Works unchanged under stream
+// capture.
+int enqueue_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
+  CK(cudaMemsetAsync(c->b.ncand, 0, sizeof(int), c->stream), "memset");
+  CK(cudaEventRecord(c->ev_fork, c->stream), "cudaEventRecord");
+  CK(cudaStreamWaitEvent(c->stream_pre, c->ev_fork, 0), "cudaStreamWaitEvent");
+  bool used[2] = {false, false};
+  for (size_t t = 0; t < hs.size(); t++) {
+    if (!hs[t].inside || hs[t].nss == 0) continue;
+    const int slot = (int)t & 1;
+    int rc = enqueue_sky(c, hs[t], o, (int)t, nullptr, 0, used[slot]);
+    if (rc) return rc;
+    used[slot] = true;
+  }
+  CK(cudaEventRecord(c->ev_join, c->stream_pre), "cudaEventRecord");
+  CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "cudaStreamWaitEvent");
+  return PA_OK;
+}
+
+// Replaces *exec by an executable graph of g: updated in place when the
+// topology matches, instantiated anew otherwise.
+int graph_exec_from(cudaGraph_t g, cudaGraphExec_t* exec, std::string* err) {
+  if (*exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(*exec, g, &info) == cudaSuccess) return PA_OK;
+    cudaGetLastError();
+    cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
+  }
+  cudaError_t e = cudaGraphInstantiate(exec, g, 0);
+  if (e != cudaSuccess) {
+    *exec = nullptr;
+    *err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e);
+    return PA_ERR_CUDA;
+  }
+  return PA_OK;
+}
+
+// Enqueues the batch directly, or captures it into the context's graph and
+// launches that.
+int launch_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
+  const bool graph = c->graphs && !c->prof.on;
+  if (!graph) return enqueue_tasks(c, hs, o);
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+  int rc = enqueue_tasks(c, hs, o);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+  rc = graph_exec_from(g, &c->gexec, &c->err);
+  cudaGraphDestroy(g);
+  if (rc) return rc;
+  CK(cudaGraphLaunch(c->gexec, c->stream), "cudaGraphLaunch");
+  return PA_OK;
+}
+
+// After the batch finished: the device candidates, sorted to the serial
+// order, into `out`; returns PA_ERR_CAPACITY (with *n the count) when the
+// device buffer overflowed.
+int collect_tasks(pa_ctx* c, std::vector<pa::DevCand>* out, int* n_out) {
+  CK(cudaMemcpyAsync(c->h_ncand, c->b.ncand, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "copy count");
+  CK(cudaStreamSynchronize(c->stream), "search");
+  const int n = *c->h_ncand;
+  *n_out = n;
+  if (n > c->b.cand_cap) return PA_ERR_CAPACITY;
+  if (n > 0) {
+    CK(cudaMemcpyAsync(c->h_cand, c->b.cand, sizeof(pa::DevCand) * (size_t)n, cudaMemcpyDeviceToHost,
+                       c->stream), "copy candidates");
+    CK(cudaStreamSynchronize(c->stream), "copy candidates");
+  }
+  out->assign(c->h_cand, c->h_cand + n);
+  std::sort(out->begin(), out->end(), cand_less);
+  return PA_OK;
+}
+
+// Grows the device candidate buffer to hold n (with margin); the engine is
+// rebuilt on the new buffers (its schedule kept) and any graph dropped.
+int grow_candidates(pa_ctx* c, int n) {
+  const int ncap = n + n / 2;
+  void* p = nullptr;
+  CK(cudaMalloc(&p, sizeof(pa::DevCand) * (size_t)ncap), "cudaMalloc");
+  c->allocs.push_back(p);
+  c->b.cand = (pa::DevCand*)p;
+  cudaFreeHost(c->h_cand);
+  c->h_cand = nullptr;
+  CK(cudaMallocHost((void**)&c->h_cand, sizeof(pa::DevCand) * (size_t)ncap), "cudaMallocHost");
+  c->b.cand_cap = ncap;
+  const long long before = c->eng->launches();
+  const int split = c->eng->split();
+  delete c->eng;
+  c->eng = c->fp64 ? pa::make_engine_f64(c->b) : pa::make_engine_f32(c->b, c->cfg.phase_mode);
+  c->eng->prof = &c->prof;
+  c->eng->set_split(split);
+  c->extra_launches += before;
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  return PA_OK;
+}
+
 // Runs the sky points, gathers the device candidates (sorted to the serial
 // order) into `out`.  Grows the device candidate buffer and re-runs when it
 // overflowed.
@@ -590,52 +714,20 @@ int run_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o, std::
   CK(cudaSetDevice(c->dev), "cudaSetDevice");
   for (int attempt = 0; attempt < 3; attempt++) {
     CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
-    CK(cudaMemsetAsync(c->b.ncand, 0, sizeof(int), c->stream), "memset");
-    // the prelude stream starts after ev0 so the timing covers its work
-    CK(cudaStreamWaitEvent(c->stream_pre, c->ev0, 0), "cudaStreamWaitEvent");
-    int nq = 0;
-    for (size_t t = 0; t < hs.size(); t++) {
-      if (!hs[t].inside || hs[t].nss == 0) continue;
-      int rc = enqueue_sky(c, hs[t], o, (int)t, nullptr, 0);
-      if (rc) return rc;
-      nq++;
-    }
-    (void)nq;
+    int rc = launch_tasks(c, hs, o);
+    if (rc) return rc;
     CK(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
-    CK(cudaMemcpyAsync(c->h_ncand, c->b.ncand, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "copy count");
-    CK(cudaStreamSynchronize(c->stream), "search");
+    int n = 0;
+    rc = collect_tasks(c, out, &n);
     {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, c->ev0, c->ev1);
       c->last_ms = ms;
     }
     if (c->prof.on) prof_collect(c);
-    const int n = *c->h_ncand;
-    if (n <= c->b.cand_cap) {
-      if (n > 0) {
-        CK(cudaMemcpyAsync(c->h_cand, c->b.cand, sizeof(pa::DevCand) * (size_t)n, cudaMemcpyDeviceToHost,
-                           c->stream), "copy candidates");
-        CK(cudaStreamSynchronize(c->stream), "copy candidates");
-      }
-      out->assign(c->h_cand, c->h_cand + n);
-      std::sort(out->begin(), out->end(), cand_less);
-      return PA_OK;
-    }
-    // grow and retry
-    const int ncap = n + n / 2;
-    void* p = nullptr;
-    CK(cudaMalloc(&p, sizeof(pa::DevCand) * (size_t)ncap), "cudaMalloc");
-    c->allocs.push_back(p);
-    c->b.cand = (pa::DevCand*)p;
-    cudaFreeHost(c->h_cand);
-    c->h_cand = nullptr;
-    CK(cudaMallocHost((void**)&c->h_cand, sizeof(pa::DevCand) * (size_t)ncap), "cudaMallocHost");
-    c->b.cand_cap = ncap;
-    const long long before = c->eng->launches();
-    delete c->eng;
-    c->eng = c->fp64 ? pa::make_engine_f64(c->b) : pa::make_engine_f32(c->b, c->cfg.phase_mode);
-    c->eng->prof = &c->prof;
-    c->extra_launches += before;
+    if (rc == PA_OK) return PA_OK;
+    if (rc != PA_ERR_CAPACITY) return rc;
+    if ((rc = grow_candidates(c, n))) return rc;
   }
   return fail(c, PA_ERR_CAPACITY, "device candidate buffer overflow");
 }
@@ -717,6 +809,79 @@ int pa_search_batch(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o
   int rc = run_tasks(c, hs, o, &cands);
   if (rc) return rc;
   return append_records(c, hs, o, cands, sgnlc, sgnlv, cap, idx, FNum, needed);
+}
+
+int pa_set_graphs(pa_ctx* c, int on) {
+  if (!c) return PA_ERR_ARG;
+  c->graphs = on != 0;
+  if (!c->graphs && c->gexec) {
+    cudaSetDevice(c->dev);
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  return PA_OK;
+}
+
+int pa_set_schedule(pa_ctx* c, int sbatch, int split) {
+  if (!c || sbatch < 1 || sbatch > c->sb_max || split < 0 || split > 1)
+    return fail(c, PA_ERR_ARG, "pa_set_schedule: sbatch must be in [1, %d], split 0 or 1", c ? c->sb_max : 0);
+  c->b.sbatch = sbatch;
+  c->eng->set_split(split);
+  return PA_OK;
+}
+
+int pa_get_schedule(const pa_ctx* c, int* sbatch, int* split, int* max_sbatch) {
+  if (!c) return PA_ERR_ARG;
+  if (sbatch) *sbatch = c->b.sbatch;
+  if (split) *split = c->eng->split();
+  if (max_sbatch) *max_sbatch = c->sb_max;
+  return PA_OK;
+}
+
+int pa_autotune(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o, const pa_range* r, int* sbatch,
+                int* split) {
+  if (!c || !tasks || ntasks < 1 || !o || !r) return fail(c, PA_ERR_ARG, "pa_autotune: bad arguments");
+  std::vector<SkyHost> hs(ntasks);
+  for (int t = 0; t < ntasks; t++)
+    sky_setup(c, tasks[t].pm, tasks[t].mm, tasks[t].nn, o, t == 0 ? r->sst : r->spndr[0], r->spndr[1], &hs[t]);
+  const int sb0 = c->b.sbatch, sp0 = c->eng->split();
+  int cands[3] = {std::max(1, c->sb_max / 4), std::max(1, c->sb_max / 2), c->sb_max};
+  // the factor split is a choice only for odd log2(nfftf)
+  const int nsplit = (c->sett.nfftf & 0xAAAAAAAA) ? 2 : 1;
+  double best = 1e300;
+  int bsb = sb0, bsp = sp0;
+  std::vector<pa::DevCand> out;
+  for (int k = 0; k < 3; k++) {
+    if (k > 0 && cands[k] == cands[k - 1]) continue;
+    for (int sp = 0; sp < nsplit; sp++) {
+      c->b.sbatch = cands[k];
+      c->eng->set_split(sp);
+      double t = 1e300;
+      for (int rep = 0; rep < 3; rep++) {  // first run warms up
+        int rc = run_tasks(c, hs, o, &out);
+        if (rc) {
+          c->b.sbatch = sb0;
+          c->eng->set_split(sp0);
+          return rc;
+        }
+        if (rep > 0) t = std::min(t, c->last_ms);
+      }
+      if (t < best) {
+        best = t;
+        bsb = cands[k];
+        bsp = sp;
+      }
+    }
+  }
+  c->b.sbatch = bsb;
+  c->eng->set_split(bsp);
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  if (sbatch) *sbatch = bsb;
+  if (split) *split = bsp;
+  return PA_OK;
 }
 
 int pa_debug_prelude(pa_ctx* c, int pm, int mm, int nn, double* xa, double* xb, double* aa, double* bb) {
@@ -1050,3 +1215,190 @@ extern "C" int pa_fstat_noalloc(const pa_settings* sett, const pa_detector* det,
 #undef NCK
   return PA_OK;
 }
+
+// ------------------------------------------------------------------
+// Multi-segment front-end: the batches of several contexts (one per data
+// segment, each with its own N and FFT lengths) enqueued together, each on
+// its own streams forked from one origin stream, optionally captured into
+// one CUDA graph and launched once.
+
+struct pa_segments {
+  std::vector<pa_ctx*> ctx;
+  int dev = 0;
+  cudaStream_t origin = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> fork, join;
+  bool graph = true;
+  cudaGraphExec_t gexec = nullptr;
+  double last_ms = 0.;
+  std::string err;
+};
+
+namespace {
+thread_local std::string g_seg_error;
+
+int seg_fail(pa_segments* s, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (s) s->err = buf;
+  else g_seg_error = buf;
+  return code;
+}
+
+#define SCK(call, what)                                                                                   \
+  do {                                                                                                    \
+    cudaError_t e_ = (call);                                                                              \
+    if (e_ != cudaSuccess) return seg_fail(sg, PA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e_));      \
+  } while (0)
+
+// Enqueues every segment's batch, forked from and joined back into the
+// origin stream.
+int seg_enqueue(pa_segments* sg, const std::vector<std::vector<SkyHost>>& hs, const pa_segment_job* jobs) {
+  for (size_t k = 0; k < sg->ctx.size(); k++) {
+    pa_ctx* c = sg->ctx[k];
+    SCK(cudaEventRecord(sg->fork[k], sg->origin), "cudaEventRecord");
+    SCK(cudaStreamWaitEvent(c->stream, sg->fork[k], 0), "cudaStreamWaitEvent");
+    int rc = enqueue_tasks(c, hs[k], jobs[k].opts);
+    if (rc) return seg_fail(sg, rc, "segment %d: %s", (int)k, c->err.c_str());
+    SCK(cudaEventRecord(sg->join[k], c->stream), "cudaEventRecord");
+    SCK(cudaStreamWaitEvent(sg->origin, sg->join[k], 0), "cudaStreamWaitEvent");
+  }
+  return PA_OK;
+}
+}  // namespace
+
+extern "C" {
+
+pa_segments* pa_segments_create(pa_ctx* const* ctxs, int nseg, int* status) {
+  if (!ctxs || nseg < 1) {
+    seg_fail(nullptr, PA_ERR_ARG, "pa_segments_create: no contexts");
+    if (status) *status = PA_ERR_ARG;
+    return nullptr;
+  }
+  for (int k = 0; k < nseg; k++)
+    if (!ctxs[k] || ctxs[k]->dev != ctxs[0]->dev) {
+      seg_fail(nullptr, PA_ERR_ARG, "pa_segments_create: context %d missing or on another device", k);
+      if (status) *status = PA_ERR_ARG;
+      return nullptr;
+    }
+  pa_segments* sg = new pa_segments();
+  sg->ctx.assign(ctxs, ctxs + nseg);
+  sg->dev = ctxs[0]->dev;
+  sg->fork.assign(nseg, nullptr);
+  sg->join.assign(nseg, nullptr);
+  auto bad = [&](cudaError_t e) {
+    g_seg_error = std::string("pa_segments_create: ") + cudaGetErrorString(e);
+    pa_segments_destroy(sg);
+    if (status) *status = PA_ERR_CUDA;
+    return (pa_segments*)nullptr;
+  };
+  cudaError_t e;
+  if ((e = cudaSetDevice(sg->dev)) != cudaSuccess) return bad(e);
+  if ((e = cudaStreamCreateWithFlags(&sg->origin, cudaStreamNonBlocking)) != cudaSuccess) return bad(e);
+  if ((e = cudaEventCreate(&sg->ev0)) != cudaSuccess) return bad(e);
+  if ((e = cudaEventCreate(&sg->ev1)) != cudaSuccess) return bad(e);
+  for (int k = 0; k < nseg; k++) {
+    if ((e = cudaEventCreateWithFlags(&sg->fork[k], cudaEventDisableTiming)) != cudaSuccess) return bad(e);
+    if ((e = cudaEventCreateWithFlags(&sg->join[k], cudaEventDisableTiming)) != cudaSuccess) return bad(e);
+  }
+  if (status) *status = PA_OK;
+  return sg;
+}
+
+void pa_segments_destroy(pa_segments* sg) {
+  if (!sg) return;
+  cudaSetDevice(sg->dev);
+  if (sg->origin) cudaStreamSynchronize(sg->origin);
+  if (sg->gexec) cudaGraphExecDestroy(sg->gexec);
+  for (cudaEvent_t e : sg->fork)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : sg->join)
+    if (e) cudaEventDestroy(e);
+  if (sg->ev0) cudaEventDestroy(sg->ev0);
+  if (sg->ev1) cudaEventDestroy(sg->ev1);
+  if (sg->origin) cudaStreamDestroy(sg->origin);
+  delete sg;
+}
+
+const char* pa_segments_last_error(const pa_segments* sg) { return sg ? sg->err.c_str() : g_seg_error.c_str(); }
+
+int pa_segments_set_graph(pa_segments* sg, int on) {
+  if (!sg) return PA_ERR_ARG;
+  sg->graph = on != 0;
+  return PA_OK;
+}
+
+double pa_segments_last_call_ms(const pa_segments* sg) { return sg ? sg->last_ms : 0.; }
+
+int pa_segments_search(pa_segments* sg, const pa_segment_job* jobs, int* status) {
+  if (!sg || !jobs) return seg_fail(sg, PA_ERR_ARG, "pa_segments_search: bad arguments");
+  const int ns = (int)sg->ctx.size();
+  for (int k = 0; k < ns; k++) {
+    const pa_segment_job& j = jobs[k];
+    if ((j.ntasks > 0 && !j.tasks) || j.ntasks < 0 || !j.opts || !j.range || !j.sgnlc || !j.sgnlv || !j.FNum ||
+        j.cap < 0)
+      return seg_fail(sg, PA_ERR_ARG, "pa_segments_search: bad job %d", k);
+  }
+  SCK(cudaSetDevice(sg->dev), "cudaSetDevice");
+  std::vector<std::vector<SkyHost>> hs(ns);
+  bool profiling = false;
+  for (int k = 0; k < ns; k++) {
+    const pa_segment_job& j = jobs[k];
+    hs[k].resize(j.ntasks);
+    for (int t = 0; t < j.ntasks; t++)
+      sky_setup(sg->ctx[k], j.tasks[t].pm, j.tasks[t].mm, j.tasks[t].nn, j.opts,
+                t == 0 ? j.range->sst : j.range->spndr[0], j.range->spndr[1], &hs[k][t]);
+    profiling |= sg->ctx[k]->prof.on;
+  }
+  SCK(cudaEventRecord(sg->ev0, sg->origin), "cudaEventRecord");
+  int rc;
+  if (sg->graph && !profiling) {
+    SCK(cudaStreamBeginCapture(sg->origin, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    rc = seg_enqueue(sg, hs, jobs);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(sg->origin, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return seg_fail(sg, PA_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+    rc = graph_exec_from(g, &sg->gexec, &sg->err);
+    cudaGraphDestroy(g);
+    if (rc) return rc;
+    SCK(cudaGraphLaunch(sg->gexec, sg->origin), "cudaGraphLaunch");
+  } else {
+    if ((rc = seg_enqueue(sg, hs, jobs))) return rc;
+  }
+  SCK(cudaEventRecord(sg->ev1, sg->origin), "cudaEventRecord");
+  SCK(cudaStreamSynchronize(sg->origin), "segments");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, sg->ev0, sg->ev1);
+  sg->last_ms = ms;
+  int worst = PA_OK;
+  for (int k = 0; k < ns; k++) {
+    pa_ctx* c = sg->ctx[k];
+    const pa_segment_job& j = jobs[k];
+    if (c->prof.on) prof_collect(c);
+    std::vector<pa::DevCand> cands;
+    int n = 0;
+    rc = collect_tasks(c, &cands, &n);
+    if (rc == PA_ERR_CAPACITY) {
+      // device buffer overflow: grow and run this segment again on its own
+      rc = grow_candidates(c, n);
+      if (rc == PA_OK) rc = run_tasks(c, hs[k], j.opts, &cands);
+    }
+    if (rc == PA_OK)
+      rc = append_records(c, hs[k], j.opts, cands, j.sgnlc, j.sgnlv, j.cap, j.idx, j.FNum, j.needed);
+    if (status) status[k] = rc;
+    if (rc && !worst) {
+      worst = rc;
+      sg->err = "segment " + std::to_string(k) + ": " + c->err;
+    }
+  }
+  return worst;
+}
+
+}  // extern "C"

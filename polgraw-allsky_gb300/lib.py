@@ -30,6 +30,9 @@ EXPORTS = [
     "pa_host_create", "pa_host_setup", "pa_host_search", "pa_host_main", "pa_host_destroy",
     "pa_host_settings", "pa_host_detectors", "pa_host_range", "pa_host_core_opts",
     "pa_host_config", "pa_host_detector_name",
+    "pa_set_graphs", "pa_set_schedule", "pa_get_schedule", "pa_autotune", "pa_segments_create",
+    "pa_segments_destroy", "pa_segments_last_error", "pa_segments_set_graph", "pa_segments_search",
+    "pa_segments_last_call_ms",
     "pa_followup_create", "pa_followup_destroy", "pa_followup_last_error", "pa_fstatnet", "pa_fstatnet_grad",
     "pa_followup_ascent", "pa_followup_simplex", "pa_followup_last_call_ms", "pa_followup_kernel_launches",
 ]
@@ -111,6 +114,20 @@ def load(path: str | None = None) -> C.CDLL:
                                    P(C.c_longlong)]
     lib.pa_fstat_noalloc.argtypes = [P(Settings), P(Detector), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                      P(Opts), C.c_int, P(C.c_double)]
+    lib.pa_set_graphs.argtypes = [C.c_void_p, C.c_int]
+    lib.pa_set_schedule.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.pa_get_schedule.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int)]
+    lib.pa_autotune.argtypes = [C.c_void_p, P(Sky), C.c_int, P(Opts), P(Range), P(C.c_int), P(C.c_int)]
+    lib.pa_segments_create.restype = C.c_void_p
+    lib.pa_segments_create.argtypes = [P(C.c_void_p), C.c_int, P(C.c_int)]
+    lib.pa_segments_destroy.argtypes = [C.c_void_p]
+    lib.pa_segments_destroy.restype = None
+    lib.pa_segments_last_error.restype = C.c_char_p
+    lib.pa_segments_last_error.argtypes = [C.c_void_p]
+    lib.pa_segments_set_graph.argtypes = [C.c_void_p, C.c_int]
+    lib.pa_segments_search.argtypes = [C.c_void_p, P(SegmentJob), P(C.c_int)]
+    lib.pa_segments_last_call_ms.restype = C.c_double
+    lib.pa_segments_last_call_ms.argtypes = [C.c_void_p]
     lib.pa_followup_create.restype = C.c_void_p
     lib.pa_followup_create.argtypes = [P(Settings), P(Detector), C.c_int, P(Config), P(C.c_int)]
     lib.pa_followup_destroy.argtypes = [C.c_void_p]
@@ -315,6 +332,28 @@ class Context:
     def last_call_ms(self) -> float:
         return float(self.lib.pa_last_call_ms(self.ctx))
 
+    def set_graphs(self, on: bool):
+        self.lib.pa_set_graphs(self.ctx, int(bool(on)))
+
+    def set_schedule(self, sbatch: int, split: int = 0):
+        rc = self.lib.pa_set_schedule(self.ctx, sbatch, split)
+        if rc != PA_OK:
+            raise SearchError("pa_set_schedule failed (%d): %s" % (rc, self.error()))
+
+    def schedule(self):
+        """(sbatch, split, max_sbatch)."""
+        a, b, m = C.c_int(0), C.c_int(0), C.c_int(0)
+        self.lib.pa_get_schedule(self.ctx, C.byref(a), C.byref(b), C.byref(m))
+        return a.value, b.value, m.value
+
+    def autotune(self, tasks, opts: Opts, rng: Range):
+        arr = (Sky * len(tasks))(*[Sky(*t) for t in tasks])
+        a, b = C.c_int(0), C.c_int(0)
+        rc = self.lib.pa_autotune(self.ctx, arr, len(tasks), C.byref(opts), C.byref(rng), C.byref(a), C.byref(b))
+        if rc != PA_OK:
+            raise SearchError("pa_autotune failed (%d): %s" % (rc, self.error()))
+        return a.value, b.value
+
     def set_profiling(self, on: bool):
         rc = self.lib.pa_set_profiling(self.ctx, 1 if on else 0)
         if rc != PA_OK:
@@ -342,6 +381,72 @@ class Context:
         if self.ctx:
             self.lib.pa_destroy(self.ctx)
             self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SegmentJob(C.Structure):
+    _fields_ = [("tasks", C.c_void_p), ("ntasks", C.c_int), ("opts", C.c_void_p), ("range", C.c_void_p),
+                ("sgnlc", C.c_void_p), ("sgnlv", C.c_void_p), ("cap", C.c_int), ("idx", C.c_void_p),
+                ("FNum", C.c_void_p), ("needed", C.c_void_p)]
+
+
+class Segments:
+    """pa_segments: several contexts (one per data segment) searched
+    together, optionally as one CUDA graph."""
+
+    def __init__(self, contexts, graph: bool = True):
+        self.lib = load()
+        self.contexts = list(contexts)
+        arr = (C.c_void_p * len(self.contexts))(*[c.ctx for c in self.contexts])
+        st = C.c_int(0)
+        self.seg = self.lib.pa_segments_create(arr, len(self.contexts), C.byref(st))
+        if not self.seg:
+            raise SearchError("pa_segments_create failed (%d): %s" %
+                              (st.value, self.lib.pa_segments_last_error(None).decode()))
+        self.lib.pa_segments_set_graph(self.seg, int(bool(graph)))
+
+    def set_graph(self, on: bool):
+        self.lib.pa_segments_set_graph(self.seg, int(bool(on)))
+
+    def search(self, task_lists, opts_list, ranges, cap: int = 1 << 18):
+        """Returns [(records, idx, FNum)] per segment."""
+        n = len(self.contexts)
+        while True:
+            keep, jobs = [], (SegmentJob * n)()
+            outs = []
+            for k in range(n):
+                tasks = task_lists[k]
+                arr = (Sky * max(1, len(tasks)))(*[Sky(*t) for t in tasks])
+                sgnlc, fnum, needed = C.c_int(0), C.c_int(0), C.c_int(0)
+                buf = np.zeros((cap, PA_NPAR))
+                idx = (CandIdx * cap)()
+                keep += [arr, sgnlc, fnum, needed, buf, idx]
+                jobs[k] = SegmentJob(C.cast(arr, C.c_void_p), len(tasks), C.addressof(opts_list[k]),
+                                     C.addressof(ranges[k]), C.addressof(sgnlc), buf.ctypes.data, cap,
+                                     C.addressof(idx), C.addressof(fnum), C.addressof(needed))
+                outs.append((sgnlc, buf, idx, fnum, needed))
+            status = (C.c_int * n)()
+            rc = self.lib.pa_segments_search(self.seg, jobs, status)
+            if rc == PA_ERR_CAPACITY:
+                cap = max(o[4].value for o in outs) + 16
+                continue
+            if rc != PA_OK:
+                raise SearchError("pa_segments_search failed (%d): %s" %
+                                  (rc, self.lib.pa_segments_last_error(self.seg).decode()))
+            return [(o[1][:o[0].value].copy(), idx_to_array(o[2], o[0].value), o[3].value) for o in outs]
+
+    def last_call_ms(self) -> float:
+        return self.lib.pa_segments_last_call_ms(self.seg)
+
+    def close(self):
+        if getattr(self, "seg", None):
+            self.lib.pa_segments_destroy(self.seg)
+            self.seg = None
 
     def __del__(self):
         try:

@@ -127,3 +127,97 @@ def candidates_around(host, inj, n: int, seed: int = 2005):
         ws.append(w)
         which.append(j)
     return np.array(pts), np.array(ws), np.array(which)
+
+
+def segment_settings(N: int, *, dt: float = 2.0, band: int = 666, fftpad: int = 2, nifo: int = 2,
+                     m5: float = -1e-9, npoints: int = 2000):
+    """pa_settings of a data segment of arbitrary length N, as
+    search_settings() (settings.c:16-81) and plan_fftw() (init.c:835-844)
+    would set them, with a sky lattice of spacing oms*sqrt(pi/npoints)."""
+    from .lib import Settings
+    s = Settings()
+    s.dt = dt
+    s.fpo = synth.fpo_default(band, dt)
+    s.B = 0.5 / dt
+    s.oms = 2. * math.pi * s.fpo * dt
+    s.omr = synth.C_OMEGA_R * dt
+    s.N = int(N)
+    s.nod = max(1, int(round(N * dt / synth.C_SIDDAY)))
+    s.nfft = 1 << int(math.ceil(math.log(N) / math.log(2.)))
+    s.s = 1
+    s.Smax = 2. * math.pi * 0.5e-8 * dt * dt
+    s.Smin = 2. * math.pi * 0.5e-9 * dt * dt
+    s.nd = 2
+    s.interpftpad = 2
+    s.fftpad = fftpad
+    s.nmin = int(fftpad * 4096 * s.B)
+    s.nmax = int((s.nfft // 2 - 4096 * s.B) * fftpad)
+    s.Ninterp = 2 * s.nfft
+    s.nfftf = fftpad * s.nfft
+    s.sepsm = math.sin(synth.C_EPSMA)
+    s.cepsm = math.cos(synth.C_EPSMA)
+    s.nifo = nifo
+    spacing = s.oms * math.sqrt(math.pi / npoints)
+    M = synth.grid_matrix(s.nfftf, s.oms, m5=m5, sky=(spacing, 0.0, 0.0, spacing))
+    for k in range(16):
+        s.M[k] = M[k]
+    s.numlines_band = 0
+    return s
+
+
+def segment_detectors(N: int, k: int, dets=("H1", "L1"), dt: float = 2.0):
+    """Noise-only data of segment k (seeds of the detector + 100 k) with the
+    synthetic ephemeris, as a pa_detector array (and the arrays it points
+    to, which must stay alive)."""
+    from .lib import make_detectors
+    xs, ps, s2, sph, cph, am = [], [], [], [], [], []
+    for d in dets:
+        x = synth.gauss_ih(synth.DEFAULT_SEED[d] + 100 * k, N) * synth.DEFAULT_SIGMA[d]
+        pos, phir, _ = synth.detssb(d, N, dt)
+        mean = x.sum() / N
+        var = ((x - mean) ** 2).sum() / (N - 1)          # var() of auxi.c:124-139
+        xs.append(x)
+        ps.append(pos)
+        s2.append(float(var))                            # no zeros: crf0 = 1
+        sph.append(math.sin(phir))
+        cph.append(math.cos(phir))
+        site = synth.SITES[d]
+        am.append(synth.rogcvir(site["ephi"], site["egam"]))
+    return make_detectors(xs, ps, s2, sph, cph, am)
+
+
+def segments(nseg: int = 24, *, nsky: int = 300, nspin: int = 150, seed: int = 2004,
+             nmin_len: int = 60000, nmax_len: int = 260000):
+    """The multi-segment workload: nseg segments of N uniform in
+    [nmin_len, nmax_len] (seed), dt=2 s, H1+L1, fftpad=2 (nfftf = 2 nfft >=
+    2N), nsky lattice sky points x nspin spindowns each.  Returns a list of
+    dicts {N, settings, dets, keep, tasks, opts, range}."""
+    from .lib import Opts, Range
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nseg):
+        N = int(rng.integers(nmin_len, nmax_len + 1))
+        s = segment_settings(N)
+        dets, keep = segment_detectors(N, k)
+        # lattice points inside the disk (jobcore.c:248), first nsky of them
+        half = int(math.ceil(math.sqrt(2000 / math.pi))) + 1
+        tasks = []
+        for mm in range(-half, half + 1):
+            for nn in range(-half, half + 1):
+                al1, al2 = nn * s.M[10] + mm * s.M[14], nn * s.M[11] + mm * s.M[15]
+                if (al1 * al1 + al2 * al2) / (s.oms * s.oms) <= 1.0:
+                    tasks.append((1, mm, nn))
+        tasks = tasks[:nsky]
+        o = Opts()
+        o.trl = 20.0
+        o.white_flag = 0
+        o.s0_flag = 0
+        o.use_range = 1
+        r = Range()
+        r.spndr[0], r.spndr[1] = 0, nspin - 1
+        r.nr[0], r.nr[1] = -half, half
+        r.mr[0], r.mr[1] = -half, half
+        r.pmr[0], r.pmr[1] = 1, 1
+        r.sst = 0
+        out.append(dict(N=N, settings=s, dets=dets, keep=keep, tasks=tasks, opts=o, range=r))
+    return out
