@@ -126,9 +126,10 @@ def l2_flush():
     del buf
 
 
-# DRAM bytes (read + write) of one spindown pass-A launch (28-29 spindowns,
-# H1+L1, N=86164, nfftf=131072) from an ncu capture of the same kernel
-PASS_A_TRAFFIC = 13.1e6
+# DRAM bytes (read + write) per spindown of the spindown pass A (H1+L1,
+# N=86164, nfftf=131072) from ncu captures of the kernel, per schedule
+# (spindowns per launch, FFT split); scaled by the spindowns of a launch
+PASS_A_TRAFFIC_PER_SPINDOWN = {(32, 0): 13.1e6 / 28.57, (64, 1): 79.02e6 / 64}
 
 
 def peaks() -> dict:
@@ -399,6 +400,7 @@ def main():
     ap.add_argument("--fp64-sky", type=int, default=48, help="sky points timed in the all-FP64 form")
     ap.add_argument("--cpu-sky", type=int, default=48, help="sky points in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--schedule", default="", help="fixed spindown schedule 'sbatch,split' (skips the autotuner)")
     ap.add_argument("--segments", type=int, default=24, help="segments workload: number of segments")
     ap.add_argument("--workload", default="network", choices=["network", "stress", "followup", "segments"],
                     help="stress: the N=258492 precision-stress workload, every precision form; "
@@ -471,7 +473,10 @@ def main():
     ctx = L.Context(s, dets, nifo, precision=L.PA_PREC_MIXED, phase_mode=phase, device=0)
     opts, rng = host.opts(), host.range
     templates = len(tasks) * nspin * bins
-    if args.autotune:
+    if args.schedule:
+        sb_, sp_ = (int(v) for v in args.schedule.split(","))
+        ctx.set_schedule(sb_, sp_)
+    elif args.autotune:
         ctx.autotune(tasks[:8], opts, rng)
     ctx.set_graphs(bool(args.graphs))
     sched = ctx.schedule()
@@ -509,7 +514,8 @@ def main():
            "clocks": clk, "gpu_launches": int(launches),
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "candidates_per_step": ncand,
-           "schedule": {"spindown_batch": sched[0], "fft_split": sched[1], "autotuned": bool(args.autotune)}}
+           "schedule": {"spindown_batch": sched[0], "fft_split": sched[1],
+                        "autotuned": bool(args.autotune) and not args.schedule}}
 
     if not args.no_extras:
         # per-kernel CUDA-event profile of one step (not the timed number)
@@ -529,8 +535,9 @@ def main():
         achieved = per_unit * items / (ms / 1e3) / 1e9 if name == "spindown_pass_a" else None
         out["roofline"] = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": pk["hbm_gbs"],
                            "unit": "GB/s", "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
-                           "traffic": PASS_A_TRAFFIC if (name == "spindown_pass_a" and s.N == 86164
-                                                          and nifo == 2) else None,
+                           "traffic": PASS_A_TRAFFIC_PER_SPINDOWN[tuple(sched[:2])] * items / max(1, nl)
+                           if (name == "spindown_pass_a" and s.N == 86164 and nifo == 2
+                               and tuple(sched[:2]) in PASS_A_TRAFFIC_PER_SPINDOWN) else None,
                            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch "
                                              "(profiles/spindown_pass_a_network_n86164.md)",
                            "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs)",

@@ -551,17 +551,39 @@ void sky_setup(const pa_ctx* c, int pm, int mm, int nn, const pa_opts* o, int ss
   a.task = 0;
 }
 
+// x mod 1 as a 64-bit fixed-point fraction (x 2^64 mod 2^64), exactly, from
+// the bits of x (the same integer algorithm as the device's turns_fixed)
+uint64_t host_turns_fixed(double x) {
+  uint64_t bits;
+  memcpy(&bits, &x, 8);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  if (e == 0) return 0;
+  const uint64_t m = (bits & 0xfffffffffffffull) | 0x10000000000000ull;
+  const int sh = e - 1011;
+  uint64_t t;
+  if (sh >= 64) t = 0;
+  else if (sh >= 0) t = m << sh;
+  else if (sh > -64) t = m >> (-sh);
+  else t = 0;
+  return (bits >> 63) ? (0 - t) : t;
+}
+
 // Kernel arguments of a sky point for this context's engine.
 pa::SkyArgs sky_args(const pa_ctx* c, const SkyHost& h, int task) {
   pa::SkyArgs a = h.args;
   a.task = task;
   a.ss_base = 0;
+  a.h0f = host_turns_fixed(a.het0 / (2. * M_PI));
+  a.oms_t = a.oms / (2. * M_PI);
+  a.s1f = a.m5f = 0;
   if (!c->fp64 && c->cfg.phase_mode == PA_PHASE_FIXED) {
     // the fixed-point phase terms are formed in turns, relative to the
     // first spindown so that the per-spindown factor is non-negative
     a.ss_base = h.smin;
     a.s1_0 = (a.s1_0 + h.smin * a.M5) / (2. * M_PI);
     a.M5 = a.M5 / (2. * M_PI);
+    a.s1f = host_turns_fixed(a.s1_0);
+    a.m5f = host_turns_fixed(a.M5);
   }
   return a;
 }
@@ -642,10 +664,14 @@ int graph_exec_from(cudaGraph_t g, cudaGraphExec_t* exec, std::string* err) {
 }
 
 // Enqueues the batch directly, or captures it into the context's graph and
-// launches that.
+// launches that.  The timing event ev0 goes on the stream right before the
+// work (after the capture and graph update, which are host work).
 int launch_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
   const bool graph = c->graphs && !c->prof.on;
-  if (!graph) return enqueue_tasks(c, hs, o);
+  if (!graph) {
+    CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
+    return enqueue_tasks(c, hs, o);
+  }
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
   int rc = enqueue_tasks(c, hs, o);
   cudaGraph_t g = nullptr;
@@ -658,6 +684,7 @@ int launch_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
   rc = graph_exec_from(g, &c->gexec, &c->err);
   cudaGraphDestroy(g);
   if (rc) return rc;
+  CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
   CK(cudaGraphLaunch(c->gexec, c->stream), "cudaGraphLaunch");
   return PA_OK;
 }
@@ -713,7 +740,6 @@ int grow_candidates(pa_ctx* c, int n) {
 int run_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o, std::vector<pa::DevCand>* out) {
   CK(cudaSetDevice(c->dev), "cudaSetDevice");
   for (int attempt = 0; attempt < 3; attempt++) {
-    CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
     int rc = launch_tasks(c, hs, o);
     if (rc) return rc;
     CK(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
@@ -1353,7 +1379,6 @@ int pa_segments_search(pa_segments* sg, const pa_segment_job* jobs, int* status)
                 t == 0 ? j.range->sst : j.range->spndr[0], j.range->spndr[1], &hs[k][t]);
     profiling |= sg->ctx[k]->prof.on;
   }
-  SCK(cudaEventRecord(sg->ev0, sg->origin), "cudaEventRecord");
   int rc;
   if (sg->graph && !profiling) {
     SCK(cudaStreamBeginCapture(sg->origin, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
@@ -1368,8 +1393,11 @@ int pa_segments_search(pa_segments* sg, const pa_segment_job* jobs, int* status)
     rc = graph_exec_from(g, &sg->gexec, &sg->err);
     cudaGraphDestroy(g);
     if (rc) return rc;
+    // timing starts at the launch (capture and update are host work)
+    SCK(cudaEventRecord(sg->ev0, sg->origin), "cudaEventRecord");
     SCK(cudaGraphLaunch(sg->gexec, sg->origin), "cudaGraphLaunch");
   } else {
+    SCK(cudaEventRecord(sg->ev0, sg->origin), "cudaEventRecord");
     if ((rc = seg_enqueue(sg, hs, jobs))) return rc;
   }
   SCK(cudaEventRecord(sg->ev1, sg->origin), "cudaEventRecord");

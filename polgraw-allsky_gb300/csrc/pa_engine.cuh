@@ -92,6 +92,16 @@ __global__ void __launch_bounds__(256)
   const int d = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   R a2r = 0, b2r = 0;
+  // FP32 forms: shft at sample 0 of this detector, by the expression every
+  // sample uses
+  __shared__ double sh1[1];
+  if (sizeof(R) == 4) {
+    if (threadIdx.x == 0) {
+      const double* D0 = DetSSB + 3 * (size_t)d * N;
+      sh1[0] = fma(sky.nS[0], D0[0], fma(sky.nS[1], D0[1], __dmul_rn(sky.nS[2], D0[2])));
+    }
+    __syncthreads();
+  }
   if (i < N) {
     const DetConst& k = dc[d];
     // modvir, settings.c:303-322
@@ -112,50 +122,60 @@ __global__ void __launch_bounds__(256)
                  k5 * sindel;
     a2r = aa * aa;
     b2r = bb * bb;
-    // shft, shftf, _tmp1 (jobcore.c:285-295), FP64 with the reference's
-    // rounding sequence (no FMA contraction): shftf[0] must be exactly 0, as
-    // shft1 comes from the same expression on the host; a contracted product
-    // would leave +-1 ulp there and push the spline abscissa 2(i - shftf)
-    // below 0, where splint returns 0 (auxi.c:89).
+    // shft, shftf, _tmp1 (jobcore.c:285-295)
     const double* D = DetSSB + 3 * ((size_t)d * N + i);
-    const double shft = __dadd_rn(__dadd_rn(__dmul_rn(sky.nS[0], D[0]), __dmul_rn(sky.nS[1], D[1])),
-                                  __dmul_rn(sky.nS[2], D[2]));
-    shftf[(size_t)d * N + i] = shft - sky.shft1[d];
-    const double di = (double)i;
-    const double tmp1 = __dadd_rn(__dmul_rn(di, di), __dmul_rn((double)(2 * i), shft));
     const size_t o = (size_t)d * N + i;
-    if (sizeof(R) == 8) {
-      reinterpret_cast<double*>(ph0)[o] = tmp1;
-    } else {
-      // FP32 forms: the phase coefficients fill the upper half of the
-      // sample's 32-byte record (the resampled data fill the lower half)
-      uint4 hi16;
-      if (PM == PM_FIXED) {
-        // spindown phase s1(ss) tmp1 = s1(ss_base) tmp1 + (ss - ss_base) (M5 tmp1);
-        // both terms as 64-bit fixed-point fractions of a turn (sky.s1_0
-        // and sky.M5 hold s1(ss_base)/2pi and M5/2pi in this mode)
-        const uint64_t A = turns_fixed(sky.s1_0 * tmp1), B = turns_fixed(sky.M5 * tmp1);
-        hi16 = make_uint4((unsigned)A, (unsigned)(A >> 32), (unsigned)B, (unsigned)(B >> 32));
-      } else if (PM == PM_FF) {
-        const float hi = (float)tmp1;
-        hi16 = make_uint4(__float_as_uint(hi), __float_as_uint((float)(tmp1 - (double)hi)), 0u, 0u);
-      } else {
-        const unsigned long long tb = (unsigned long long)__double_as_longlong(tmp1);
-        hi16 = make_uint4((unsigned)tb, (unsigned)(tb >> 32), 0u, 0u);
-      }
-      reinterpret_cast<uint4*>(ph0)[2 * o + 1] = hi16;
-    }
-    // prelude phase het0 i + oms shft (jobcore.c:299), FP64
-    const double phase = __dadd_rn(__dmul_rn(sky.het0, di), __dmul_rn(sky.oms, shft));
+    const double di = (double)i;
     R sp, cp;
     if (sizeof(R) == 8) {
+      // FP64 form: the reference's rounding sequence (no FMA contraction):
+      // shftf[0] must be exactly 0, as shft1 comes from the same expression
+      // on the host; a contracted product would leave +-1 ulp there and push
+      // the spline abscissa 2(i - shftf) below 0, where splint returns 0
+      // (auxi.c:89).
+      const double shft = __dadd_rn(__dadd_rn(__dmul_rn(sky.nS[0], D[0]), __dmul_rn(sky.nS[1], D[1])),
+                                    __dmul_rn(sky.nS[2], D[2]));
+      shftf[o] = shft - sky.shft1[d];
+      const double tmp1 = __dadd_rn(__dmul_rn(di, di), __dmul_rn((double)(2 * i), shft));
+      reinterpret_cast<double*>(ph0)[o] = tmp1;
+      // prelude phase het0 i + oms shft (jobcore.c:299), FP64
+      const double phase = __dadd_rn(__dmul_rn(sky.het0, di), __dmul_rn(sky.oms, shft));
       double sd, cd;
       sincos(phase, &sd, &cd);
       sp = (R)sd;
       cp = (R)cd;
     } else {
-      // reduce in turns: exact fraction from the FP64 value, then FP32
-      const uint64_t t = turns_fixed(phase * kInvTwoPi);
+      // FP32 forms: shft with fused multiply-adds; shft1 is the same
+      // expression at sample 0 (sh1, below), so shftf[0] is exactly 0
+      const double shft = fma(sky.nS[0], D[0], fma(sky.nS[1], D[1], __dmul_rn(sky.nS[2], D[2])));
+      shftf[o] = shft - sh1[0];
+      // 2 i shft, the non-integer part of _tmp1 = i^2 + 2 i shft
+      const double p2 = __dmul_rn(di + di, shft);
+      const uint64_t ii2 = (uint64_t)i * (uint64_t)i;
+      // the phase coefficients fill the upper half of the sample's 32-byte
+      // record (the resampled data fill the lower half)
+      uint4 hi16;
+      if (PM == PM_FIXED) {
+        // spindown phase s1(ss) tmp1 = s1(ss_base) tmp1 + (ss - ss_base) (M5 tmp1)
+        // as 64-bit fixed-point turns: the i^2 part exactly in integers from
+        // the fixed-point coefficients, the 2 i shft part from its FP64 value
+        const uint64_t A = sky.s1f * ii2 + turns_fixed(sky.s1_0 * p2);
+        const uint64_t B = sky.m5f * ii2 + turns_fixed(sky.M5 * p2);
+        hi16 = make_uint4((unsigned)A, (unsigned)(A >> 32), (unsigned)B, (unsigned)(B >> 32));
+      } else {
+        const double tmp1 = (double)ii2 + p2;
+        if (PM == PM_FF) {
+          const float hi = (float)tmp1;
+          hi16 = make_uint4(__float_as_uint(hi), __float_as_uint((float)(tmp1 - (double)hi)), 0u, 0u);
+        } else {
+          const unsigned long long tb = (unsigned long long)__double_as_longlong(tmp1);
+          hi16 = make_uint4((unsigned)tb, (unsigned)(tb >> 32), 0u, 0u);
+        }
+      }
+      reinterpret_cast<uint4*>(ph0)[2 * o + 1] = hi16;
+      // prelude phase het0 i + oms shft (jobcore.c:299) in fixed-point
+      // turns: het0/2pi exactly in integers, oms shft/2pi from its FP64 value
+      const uint64_t t = sky.h0f * (uint64_t)i + turns_fixed(sky.oms_t * shft);
       float sf, cf;
       sincospif((float)(int)(t >> 32) * 4.656612873077393e-10f, &sf, &cf);
       sp = (R)sf;
@@ -418,7 +438,54 @@ template <typename R> struct FstatStore {
 };
 
 // ------------------------------------------------------------------
-// spline (auxi.c:56-81): chunked FP64 recurrences.  The forward sweep
+// Compensated two-float (float-float) arithmetic for the spline recurrences
+// of the FP32 forms: a value is hi + lo with |lo| <= ulp(hi)/2 (about 48
+// significant bits).  Products use fmaf for their exact error terms; the
+// explicit __fmul_rn keeps the compiler from fusing a rounded product into
+// the following sum.
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_split(double x) {
+  const float h = (float)x;
+  return FF{h, (float)(x - (double)h)};
+}
+
+// a*x + t, a a float-float constant, t a float (Dekker/Knuth error-free
+// transformations: the product error by fma, the sum error by TwoSum)
+__device__ __forceinline__ FF ff_axpt(FF a, FF x, float t) {
+  const float p = __fmul_rn(a.hi, x.hi);
+  float e = __fmaf_rn(a.hi, x.hi, -p);
+  e = __fmaf_rn(a.hi, x.lo, e);
+  e = __fmaf_rn(a.lo, x.hi, e);
+  const float s = __fadd_rn(p, t);
+  const float bb = __fsub_rn(s, p);
+  const float r = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bb)), __fsub_rn(t, bb));
+  const float c = __fadd_rn(r, e);
+  const float hi = __fadd_rn(s, c);
+  return FF{hi, __fsub_rn(c, __fsub_rn(hi, s))};
+}
+
+// a*x + y, a a float-float constant, x and y float-float
+__device__ __forceinline__ FF ff_axpy(FF a, FF x, FF y) {
+  const float p = __fmul_rn(a.hi, x.hi);
+  float e = __fmaf_rn(a.hi, x.hi, -p);
+  e = __fmaf_rn(a.hi, x.lo, e);
+  e = __fmaf_rn(a.lo, x.hi, e);
+  const float s = __fadd_rn(p, y.hi);
+  const float bb = __fsub_rn(s, p);
+  float r = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bb)), __fsub_rn(y.hi, bb));
+  r = __fadd_rn(r, __fadd_rn(e, y.lo));
+  const float hi = __fadd_rn(s, r);
+  return FF{hi, __fsub_rn(r, __fsub_rn(hi, s))};
+}
+
+// ------------------------------------------------------------------
+// spline (auxi.c:56-81): chunked recurrences, FP64 in the FP64 form and
+// compensated two-float in the FP32 forms (the FP64 pipe of a GB300 runs at
+// 1/64 of the FP32 rate, and these sweeps are its largest user in the
+// prelude).  The forward sweep
 // u_i = (-u_{i-1}/2 + 3 d_i) invp_i has |dU_i/dU_{i-1}| -> 2 - sqrt(3) = 0.268
 // and the back substitution y2_k = p_k y2_{k+1} + u_k likewise, so a chunk
 // can start kWarm steps early from zero: the start error shrinks by
@@ -457,22 +524,43 @@ __global__ void __launch_bounds__(kSplineThreads)
   if (threadIdx.x < kSplineChunks) {
     const int lo = seg0 + threadIdx.x * kSplineChunk;
     const int hi = min(lo + kSplineChunk, n - 1);
-    // u_i = (-u_{i-1}/2 + 3 d_i) invp_i = al_i u_{i-1} + be_i d_i in FP64;
-    // the second difference d_i of the working-precision data is formed in
-    // that precision (its rounding is below the data's own)
+    // u_i = (-u_{i-1}/2 + 3 d_i) invp_i = al_i u_{i-1} + be_i d_i; the
+    // second difference d_i of the working-precision data is formed in that
+    // precision (its rounding is below the data's own)
     int i = max(1, lo - kSplineWarm);
-    double ux = 0., uy = 0.;
     T p = ys[i - 1 - y0], cc = ys[i - y0];
-    for (; i < hi; ++i) {
-      const T nn = ys[i + 1 - y0];
-      const R dx = p.x - (R)2 * cc.x + nn.x, dy = p.y - (R)2 * cc.y + nn.y;
-      const int ti = i < 64 ? i : 63;
-      const double al = -.5 * invp[ti], be = 3. * invp[ti];
-      ux = fma(al, ux, be * (double)dx);
-      uy = fma(al, uy, be * (double)dy);
-      if (i >= lo) us[i - seg0] = make_double2(ux, uy);
-      p = cc;
-      cc = nn;
+    if (sizeof(R) == 8) {
+      double ux = 0., uy = 0.;
+      for (; i < hi; ++i) {
+        const T nn = ys[i + 1 - y0];
+        const R dx = p.x - (R)2 * cc.x + nn.x, dy = p.y - (R)2 * cc.y + nn.y;
+        const int ti = i < 64 ? i : 63;
+        const double al = -.5 * invp[ti], be = 3. * invp[ti];
+        ux = fma(al, ux, be * (double)dx);
+        uy = fma(al, uy, be * (double)dy);
+        if (i >= lo) us[i - seg0] = make_double2(ux, uy);
+        p = cc;
+        cc = nn;
+      }
+    } else {
+      FF ux{0.f, 0.f}, uy{0.f, 0.f};
+      float4* us4 = reinterpret_cast<float4*>(us);
+      auto step = [&](FF al, float be) {
+        const T nn = ys[i + 1 - y0];
+        const float dx = (float)(p.x - (R)2 * cc.x + nn.x), dy = (float)(p.y - (R)2 * cc.y + nn.y);
+        ux = ff_axpt(al, ux, __fmul_rn(be, dx));
+        uy = ff_axpt(al, uy, __fmul_rn(be, dy));
+        if (i >= lo) us4[i - seg0] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
+        p = cc;
+        cc = nn;
+      };
+      // the first 63 steps of the array have their own coefficients; from
+      // i = 63 on they are constant (two loops keep the FP64 table reads out
+      // of the main one)
+      for (; i < hi && i < 63; ++i) step(ff_split(-.5 * invp[i]), (float)(3. * invp[i]));
+      const FF al = ff_split(-.5 * invp[63]);
+      const float be = (float)(3. * invp[63]);
+      for (; i < hi; ++i) step(al, be);
     }
     if (lo == 0) us[0] = make_double2(0., 0.);
   }
@@ -502,13 +590,29 @@ __global__ void __launch_bounds__(kSplineThreads)
   const int hi = min(lo + kSplineChunk, n);
   if (threadIdx.x < kSplineChunks && lo < n) {
     const int kst = min(n - 2, hi - 1 + kSplineWarm);
-    double vx = 0., vy = 0.;
-    for (int k = kst; k >= lo; --k) {
-      const double p = ptab[k < 64 ? k : 63];
-      const double2 uk = us[k - seg0];
-      vx = p * vx + uk.x;
-      vy = p * vy + uk.y;
-      if (k < hi) ys[k - seg0] = mk((R)vx, (R)vy);
+    if (sizeof(R) == 8) {
+      double vx = 0., vy = 0.;
+      for (int k = kst; k >= lo; --k) {
+        const double p = ptab[k < 64 ? k : 63];
+        const double2 uk = us[k - seg0];
+        vx = p * vx + uk.x;
+        vy = p * vy + uk.y;
+        if (k < hi) ys[k - seg0] = mk((R)vx, (R)vy);
+      }
+    } else {
+      const float4* us4 = reinterpret_cast<const float4*>(us);
+      FF vx{0.f, 0.f}, vy{0.f, 0.f};
+      int k = kst;
+      auto step = [&](FF pc) {
+        const float4 uk = us4[k - seg0];
+        vx = ff_axpy(pc, vx, FF{uk.x, uk.y});
+        vy = ff_axpy(pc, vy, FF{uk.z, uk.w});
+        if (k < hi) ys[k - seg0] = mk((R)vx.hi, (R)vy.hi);
+      };
+      // constant coefficient down to k = 64, then the table
+      const FF pc63 = ff_split(ptab[63]);
+      for (; k >= lo && k >= 64; --k) step(pc63);
+      for (; k >= lo; --k) step(ff_split(ptab[k]));
     }
     if (hi == n) ys[n - 1 - seg0] = mk((R)0, (R)0);
   }

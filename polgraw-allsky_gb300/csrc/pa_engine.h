@@ -29,6 +29,12 @@ struct SkyArgs {
   double M5;              // spindown step (0 with --nospindown); over 2 pi
                           // in the fixed-point phase mode
   double M0, M4;          // frequency step, het1 step
+  // FP32 forms: the prelude and spindown phase terms as exact 64-bit
+  // fixed-point turns of the FP64 values (turns_fixed)
+  unsigned long long h0f; // het0 / 2 pi
+  unsigned long long s1f; // s1_0 (already over 2 pi), fixed-point phase mode
+  unsigned long long m5f; // M5 (already over 2 pi), fixed-point phase mode
+  double oms_t;           // oms / 2 pi
   int ss_base;            // first spindown of the sky point (fixed-point form)
   int task;               // index of the sky point in the current batch
 };

@@ -43,7 +43,7 @@ typedef struct pa_cmdline {
   double trl, narrowdown;
   char prefix[512], dtaprefix[512], label[512], range[512], getrange[512],
       qname[512], usedet[32], addsig[512], wd[512];
-  int precision, phase_mode, sbatch, skybatch, device;
+  int precision, phase_mode, sbatch, skybatch, device, graphs;
 } pa_cmdline;
 
 typedef struct host_det {
@@ -100,7 +100,8 @@ static void print_help(void) {
   printf("-phase        spindown phase form in the mixed precision: f64, fixed (default), ff\n");
   printf("-sbatch       spindowns per fused launch (default: automatic)\n");
   printf("-skybatch     sky points per batched call (default 1)\n");
-  printf("-device       CUDA device ordinal (default 0)\n\n");
+  printf("-device       CUDA device ordinal (default 0)\n");
+  printf("-graphs       1: capture each batch of sky points into a CUDA graph (default 0)\n\n");
   printf("Also:\n\n");
   printf("--whitenoise      White Gaussian noise assumed\n");
   printf("--nospindown      Spindowns neglected\n");
@@ -151,6 +152,7 @@ static int handle_opts(pa_host *h, int argc, char **argv) {
       {"sbatch", required_argument, 0, 1003},
       {"skybatch", required_argument, 0, 1004},
       {"device", required_argument, 0, 1005},
+      {"graphs", required_argument, 0, 1006},
       {0, 0, 0, 0}};
   optind = 1;
   while (1) {
@@ -192,6 +194,7 @@ static int handle_opts(pa_host *h, int argc, char **argv) {
       case 1003: o->sbatch = atoi(optarg); break;
       case 1004: o->skybatch = atoi(optarg) > 0 ? atoi(optarg) : 1; break;
       case 1005: o->device = atoi(optarg); break;
+      case 1006: o->graphs = atoi(optarg) != 0; break;
       default: break;
     }
   }
@@ -1111,6 +1114,7 @@ int pa_host_main(int argc, char **argv) {
     pa_host_destroy(h);
     return 1;
   }
+  if (h->opts.graphs) pa_set_graphs(ctx, 1);
   rc = pa_host_search(h, ctx);
   pa_destroy(ctx);
   if (rc == PA_HOST_OK && h->opts.checkp_flag) {

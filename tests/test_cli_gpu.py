@@ -15,15 +15,18 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name", ["h1_addsig", "h1l1_gaps_veto", "h1_fullgrid"])
-@pytest.mark.parametrize("skybatch", ["1", "7"])
+@pytest.mark.parametrize("skybatch", ["1", "7", "7g"])
 def test_cli_trigger_files(name, skybatch, tmp_path, lib, gpu_ok):
+    """'7g': 7 sky points per batch, each batch captured as a CUDA graph."""
     from polgraw_gb300 import build
     g = golden(name)
     data = str(tmp_path / "data")
     os.makedirs(data)
     m = materialize(case_by_name(name), data)
     out = str(tmp_path / "out")
-    cmd = [build.EXE] + m["args"] + ["-output", out, "-skybatch", skybatch]
+    cmd = [build.EXE] + m["args"] + ["-output", out, "-skybatch", skybatch.rstrip("g")]
+    if skybatch.endswith("g"):
+        cmd += ["-graphs", "1"]
     r = subprocess.run(cmd, cwd=str(tmp_path), capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     assert sorted(os.path.basename(p) for p in glob.glob(out + "/*")) == g["trigger_files"]
