@@ -181,6 +181,8 @@ static void set_det_consts(pa_ctx* c, const pa_detector* det) {
     d.inv_sig2 = 1.0 / det[n].sig2;
     d.sphir = det[n].sphir;
     d.cphir = det[n].cphir;
+    for (int k = 0; k < 9; k++) d.amod_f[k] = (float)d.amod[k];
+    d.inv_sig2_f = (float)d.inv_sig2;
     for (int k = 0; k < 3; k++) c->det0[n][k] = det[n].DetSSB[k];
   }
 }
@@ -575,6 +577,12 @@ pa::SkyArgs sky_args(const pa_ctx* c, const SkyHost& h, int task) {
   a.ss_base = 0;
   a.h0f = host_turns_fixed(a.het0 / (2. * M_PI));
   a.oms_t = a.oms / (2. * M_PI);
+  for (int n = 0; n < pa::kMaxDet; n++) {
+    a.cosalfr_f[n] = (float)a.cosalfr[n];
+    a.sinalfr_f[n] = (float)a.sinalfr[n];
+  }
+  a.cosdel_f = (float)a.cosdel;
+  a.sindel_f = (float)a.sindel;
   a.s1f = a.m5f = 0;
   if (!c->fp64 && c->cfg.phase_mode == PA_PHASE_FIXED) {
     // the fixed-point phase terms are formed in turns, relative to the

@@ -105,16 +105,21 @@ __global__ void __launch_bounds__(256)
   if (i < N) {
     const DetConst& k = dc[d];
     // modvir, settings.c:303-322
-    const R cosalfr = (R)sky.cosalfr[d], sinalfr = (R)sky.sinalfr[d];
+    // FP32 forms read the FP32 copies: no double-to-float conversion per
+    // thread (conversions run on the FP64 pipe)
+    const bool f32 = sizeof(R) == 4;
+    const R cosalfr = f32 ? (R)sky.cosalfr_f[d] : (R)sky.cosalfr[d];
+    const R sinalfr = f32 ? (R)sky.sinalfr_f[d] : (R)sky.sinalfr[d];
     const R cm = cosmodf[i], sm = sinmodf[i];
     const R c = cosalfr * cm + sinalfr * sm;
     const R s = sinalfr * cm - cosalfr * sm;
-    const R cosdel = (R)sky.cosdel, sindel = (R)sky.sindel;
+    const R cosdel = f32 ? (R)sky.cosdel_f : (R)sky.cosdel, sindel = f32 ? (R)sky.sindel_f : (R)sky.sindel;
     const R c2d = cosdel * cosdel, c2sd = sindel * cosdel;
     const R c2s = (R)2 * c * c, cs = c * s;
-    const R k0 = (R)k.amod[0], k1 = (R)k.amod[1], k2 = (R)k.amod[2], k3 = (R)k.amod[3],
-            k4 = (R)k.amod[4], k5 = (R)k.amod[5], k6 = (R)k.amod[6], k7 = (R)k.amod[7],
-            k8 = (R)k.amod[8];
+#define PA_AMOD(j) (f32 ? (R)k.amod_f[j] : (R)k.amod[j])
+    const R k0 = PA_AMOD(0), k1 = PA_AMOD(1), k2 = PA_AMOD(2), k3 = PA_AMOD(3), k4 = PA_AMOD(4),
+            k5 = PA_AMOD(5), k6 = PA_AMOD(6), k7 = PA_AMOD(7), k8 = PA_AMOD(8);
+#undef PA_AMOD
     const R two_m = (R)2 - c2d;
     const R aa = k0 * two_m * c2s + k1 * two_m * (R)2 * cs + k2 * c2sd * c + k3 * c2sd * s -
                  k0 * two_m + k4 * c2d;
@@ -497,6 +502,13 @@ constexpr int kSplineChunks = 64;                          // recurrence threads
 constexpr int kSplineThreads = 256;                        // threads for staging loads/stores
 constexpr int kSplineSeg = kSplineChunk * kSplineChunks;   // elements per CTA
 
+// Shared-memory slot of staged element k: one padding element per chunk, so
+// that the recurrence threads (chunk starts kSplineChunk elements apart) hit
+// different banks.
+__device__ __forceinline__ int spad(int k) { return k + (k >> 6); }
+__host__ __device__ constexpr int spad_len(int n) { return n + (n >> 6) + 1; }
+static_assert(kSplineChunk == 64, "spad assumes 64-element chunks");
+
 // Forward sweep.  A CTA owns one segment of kSplineSeg elements of one
 // array; it stages y[seg - warm - 1, seg_end + 1) in shared memory with
 // coalesced loads (as FP64), every thread runs its chunk's recurrence from
@@ -508,17 +520,21 @@ __global__ void __launch_bounds__(kSplineThreads)
                  const double* __restrict__ invp) {
   typedef typename CT<R>::T T;
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  double2* us = reinterpret_cast<double2*>(sm_raw);           // kSplineSeg
-  T* ys = reinterpret_cast<T*>(us + kSplineSeg);              // kSplineSeg + kSplineWarm + 2
+  double2* us = reinterpret_cast<double2*>(sm_raw);                 // spad_len(kSplineSeg)
+  T* ys = reinterpret_cast<T*>(us + spad_len(kSplineSeg));          // spad_len(kSplineSeg + kSplineWarm + 2)
   const int q = blockIdx.x / nseg, sg = blockIdx.x - q * nseg;
   const T* yq = y + (size_t)q * ldy;
   double2* uq = u + (size_t)q * n;
   const int seg0 = sg * kSplineSeg;
   const int y0 = seg0 - kSplineWarm - 1;                       // first staged index
   const int ny = kSplineSeg + kSplineWarm + 2;
+  // the 64 pivots of the start of the array, in shared memory (the first
+  // chunk's recurrence reads one per step)
+  __shared__ double tab[64];
+  if (threadIdx.x < 64) tab[threadIdx.x] = invp[threadIdx.x];
   for (int k = threadIdx.x; k < ny; k += kSplineThreads) {
     const int i = y0 + k;
-    ys[k] = (i >= 0 && i < n) ? yq[i] : mk((R)0, (R)0);
+    ys[spad(k)] = (i >= 0 && i < n) ? yq[i] : mk((R)0, (R)0);
   }
   __syncthreads();
   if (threadIdx.x < kSplineChunks) {
@@ -528,17 +544,17 @@ __global__ void __launch_bounds__(kSplineThreads)
     // second difference d_i of the working-precision data is formed in that
     // precision (its rounding is below the data's own)
     int i = max(1, lo - kSplineWarm);
-    T p = ys[i - 1 - y0], cc = ys[i - y0];
+    T p = ys[spad(i - 1 - y0)], cc = ys[spad(i - y0)];
     if (sizeof(R) == 8) {
       double ux = 0., uy = 0.;
       for (; i < hi; ++i) {
-        const T nn = ys[i + 1 - y0];
+        const T nn = ys[spad(i + 1 - y0)];
         const R dx = p.x - (R)2 * cc.x + nn.x, dy = p.y - (R)2 * cc.y + nn.y;
         const int ti = i < 64 ? i : 63;
-        const double al = -.5 * invp[ti], be = 3. * invp[ti];
+        const double al = -.5 * tab[ti], be = 3. * tab[ti];
         ux = fma(al, ux, be * (double)dx);
         uy = fma(al, uy, be * (double)dy);
-        if (i >= lo) us[i - seg0] = make_double2(ux, uy);
+        if (i >= lo) us[spad(i - seg0)] = make_double2(ux, uy);
         p = cc;
         cc = nn;
       }
@@ -546,27 +562,27 @@ __global__ void __launch_bounds__(kSplineThreads)
       FF ux{0.f, 0.f}, uy{0.f, 0.f};
       float4* us4 = reinterpret_cast<float4*>(us);
       auto step = [&](FF al, float be) {
-        const T nn = ys[i + 1 - y0];
+        const T nn = ys[spad(i + 1 - y0)];
         const float dx = (float)(p.x - (R)2 * cc.x + nn.x), dy = (float)(p.y - (R)2 * cc.y + nn.y);
         ux = ff_axpt(al, ux, __fmul_rn(be, dx));
         uy = ff_axpt(al, uy, __fmul_rn(be, dy));
-        if (i >= lo) us4[i - seg0] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
+        if (i >= lo) us4[spad(i - seg0)] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
         p = cc;
         cc = nn;
       };
       // the first 63 steps of the array have their own coefficients; from
       // i = 63 on they are constant (two loops keep the FP64 table reads out
       // of the main one)
-      for (; i < hi && i < 63; ++i) step(ff_split(-.5 * invp[i]), (float)(3. * invp[i]));
-      const FF al = ff_split(-.5 * invp[63]);
-      const float be = (float)(3. * invp[63]);
+      for (; i < hi && i < 63; ++i) step(ff_split(-.5 * tab[i]), (float)(3. * tab[i]));
+      const FF al = ff_split(-.5 * tab[63]);
+      const float be = (float)(3. * tab[63]);
       for (; i < hi; ++i) step(al, be);
     }
-    if (lo == 0) us[0] = make_double2(0., 0.);
+    if (lo == 0) us[spad(0)] = make_double2(0., 0.);
   }
   __syncthreads();
   const int cnt = min(kSplineSeg, n - 1 - seg0);
-  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) uq[seg0 + k] = us[k];
+  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) uq[seg0 + k] = us[spad(k)];
 }
 
 // Back substitution, same staging: u[seg0, seg_end + warm) in shared memory,
@@ -577,14 +593,16 @@ __global__ void __launch_bounds__(kSplineThreads)
                  const double* __restrict__ ptab) {
   typedef typename CT<R>::T T;
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  double2* us = reinterpret_cast<double2*>(sm_raw);           // kSplineSeg + kSplineWarm
-  T* ys = reinterpret_cast<T*>(us + kSplineSeg + kSplineWarm);  // kSplineSeg
+  double2* us = reinterpret_cast<double2*>(sm_raw);                     // spad_len(kSplineSeg + kSplineWarm)
+  T* ys = reinterpret_cast<T*>(us + spad_len(kSplineSeg + kSplineWarm));  // spad_len(kSplineSeg)
   const int q = blockIdx.x / nseg, sg = blockIdx.x - q * nseg;
   const double2* uq = u + (size_t)q * n;
   T* yq = y2 + (size_t)q * n;
   const int seg0 = sg * kSplineSeg;
   const int nu = min(kSplineSeg + kSplineWarm, n - 1 - seg0);  // u defined on [0, n-2]
-  for (int k = threadIdx.x; k < nu; k += kSplineThreads) us[k] = uq[seg0 + k];
+  __shared__ double tab[64];
+  if (threadIdx.x < 64) tab[threadIdx.x] = ptab[threadIdx.x];
+  for (int k = threadIdx.x; k < nu; k += kSplineThreads) us[spad(k)] = uq[seg0 + k];
   __syncthreads();
   const int lo = seg0 + threadIdx.x * kSplineChunk;
   const int hi = min(lo + kSplineChunk, n);
@@ -593,32 +611,32 @@ __global__ void __launch_bounds__(kSplineThreads)
     if (sizeof(R) == 8) {
       double vx = 0., vy = 0.;
       for (int k = kst; k >= lo; --k) {
-        const double p = ptab[k < 64 ? k : 63];
-        const double2 uk = us[k - seg0];
+        const double p = tab[k < 64 ? k : 63];
+        const double2 uk = us[spad(k - seg0)];
         vx = p * vx + uk.x;
         vy = p * vy + uk.y;
-        if (k < hi) ys[k - seg0] = mk((R)vx, (R)vy);
+        if (k < hi) ys[spad(k - seg0)] = mk((R)vx, (R)vy);
       }
     } else {
       const float4* us4 = reinterpret_cast<const float4*>(us);
       FF vx{0.f, 0.f}, vy{0.f, 0.f};
       int k = kst;
       auto step = [&](FF pc) {
-        const float4 uk = us4[k - seg0];
+        const float4 uk = us4[spad(k - seg0)];
         vx = ff_axpy(pc, vx, FF{uk.x, uk.y});
         vy = ff_axpy(pc, vy, FF{uk.z, uk.w});
-        if (k < hi) ys[k - seg0] = mk((R)vx.hi, (R)vy.hi);
+        if (k < hi) ys[spad(k - seg0)] = mk((R)vx.hi, (R)vy.hi);
       };
       // constant coefficient down to k = 64, then the table
-      const FF pc63 = ff_split(ptab[63]);
+      const FF pc63 = ff_split(tab[63]);
       for (; k >= lo && k >= 64; --k) step(pc63);
-      for (; k >= lo; --k) step(ff_split(ptab[k]));
+      for (; k >= lo; --k) step(ff_split(tab[k]));
     }
-    if (hi == n) ys[n - 1 - seg0] = mk((R)0, (R)0);
+    if (hi == n) ys[spad(n - 1 - seg0)] = mk((R)0, (R)0);
   }
   __syncthreads();
   const int cnt = min(kSplineSeg, n - seg0);
-  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) yq[seg0 + k] = ys[k];
+  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) yq[seg0 + k] = ys[spad(k)];
 }
 
 // splint at x = interpftpad (i - shftf_i) (auxi.c:83-122), then / sig2
@@ -633,7 +651,7 @@ __global__ void __launch_bounds__(256)
   if (i >= N) return;
   const int n = 2 * N;
   const double x = __dmul_rn(2.0, __dsub_rn((double)i, shftf[(size_t)d * N + i]));
-  const R is2 = (R)dc[d].inv_sig2;
+  const R is2 = sizeof(R) == 4 ? (R)dc[d].inv_sig2_f : (R)dc[d].inv_sig2;
   T out[2];
   for (int arr = 0; arr < 2; ++arr) {
     const size_t q = (size_t)d * 2 + arr;
@@ -959,8 +977,9 @@ template <typename R, int PM> class EngineT : public Engine {
     // spline through the first 2N points of each resampled array
     const int n = 2 * N;
     const int nseg = (n + kSplineSeg - 1) / kSplineSeg;
-    const int smf = kSplineSeg * (int)sizeof(double2) + (kSplineSeg + kSplineWarm + 2) * (int)sizeof(T);
-    const int smb = (kSplineSeg + kSplineWarm) * (int)sizeof(double2) + kSplineSeg * (int)sizeof(T);
+    const int smf = spad_len(kSplineSeg) * (int)sizeof(double2) +
+                    spad_len(kSplineSeg + kSplineWarm + 2) * (int)sizeof(T);
+    const int smb = spad_len(kSplineSeg + kSplineWarm) * (int)sizeof(double2) + spad_len(kSplineSeg) * (int)sizeof(T);
     static bool donef = false, doneb = false;
     smem_attr(k_spline_fwd<R>, smf, donef);
     smem_attr(k_spline_bwd<R>, smb, doneb);

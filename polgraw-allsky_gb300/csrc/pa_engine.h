@@ -13,6 +13,7 @@ struct DetConst {
   double amod[9];
   double sig2, inv_sig2;
   double sphir, cphir;
+  float amod_f[9], inv_sig2_f;  // FP32 copies (no per-thread conversions)
 };
 
 // Per-sky-point scalars, computed on the host in FP64 exactly as
@@ -35,6 +36,7 @@ struct SkyArgs {
   unsigned long long s1f; // s1_0 (already over 2 pi), fixed-point phase mode
   unsigned long long m5f; // M5 (already over 2 pi), fixed-point phase mode
   double oms_t;           // oms / 2 pi
+  float cosalfr_f[kMaxDet], sinalfr_f[kMaxDet], cosdel_f, sindel_f;  // FP32 copies
   int ss_base;            // first spindown of the sky point (fixed-point form)
   int task;               // index of the sky point in the current batch
 };

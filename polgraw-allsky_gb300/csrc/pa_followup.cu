@@ -43,6 +43,23 @@ constexpr int kCandPerCta = 8 * kCandPerWarp;
 constexpr int kCoef = 20;         // modvir factors per point and detector
 constexpr double kInv2Pi = 0.15915494309189533577;  // 1/(2 pi), rounded to double
 
+// x mod 1 as a 64-bit fixed-point fraction (x 2^64 mod 2^64), exactly, with
+// integer operations on the bits of x: x = m 2^(e-1075), so the fraction is
+// m shifted by e - 1011, negated for x < 0.
+__device__ __forceinline__ unsigned long long fu_turns_fixed(double x) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7ff);
+  if (e == 0) return 0ull;
+  const unsigned long long m = (bits & 0xfffffffffffffull) | 0x10000000000000ull;
+  const int sh = e - 1011;
+  unsigned long long t;
+  if (sh >= 64) t = 0ull;
+  else if (sh >= 0) t = m << sh;
+  else if (sh > -64) t = m >> (-sh);
+  else t = 0ull;
+  return (bits >> 63) ? (0ull - t) : t;
+}
+
 thread_local std::string g_fu_create_error;
 
 // Per-point scalars.  Phase terms in FP64; everything else in the working
@@ -50,8 +67,12 @@ thread_local std::string g_fu_create_error;
 template <typename R>
 struct FuCand {
   double f, s;          // sgnlo[0], sgnlo[1] (radians)
-  double ft, st, st2;   // f/2pi, s/2pi, 2s/2pi (turns; mixed form)
+  // mixed form, phase in turns: f i/2pi + s i^2/2pi as 64-bit fixed point
+  // (exact integer products), (f + oms + 2 s i) shft/2pi from FP64
+  unsigned long long ffx, sfx;  // f/2pi, s/2pi in fixed-point turns
+  double fo_t, st2;     // (f + oms)/2pi, 2s/2pi
   double nS[3];         // source unit vector
+  float nSf[3];         // FP32 copy (derivative factors)
   R nD[3], nA[3];       // d nS / d delta, d nS / d alpha
   R om0, s2;            // f + oms, 2 s (d phase / d shft = om0 + s2 i)
   // adjoint seeds: conj(X) parts and the factors of dF/dX, dF/dA
@@ -93,12 +114,14 @@ __global__ void k_fu_prep(const double* __restrict__ pts, int n, const unsigned 
   sincos(de, &sd, &cd);
   c.f = f;
   c.s = s;
-  c.ft = f * kInv2Pi;
-  c.st = s * kInv2Pi;
+  c.ffx = fu_turns_fixed(f * kInv2Pi);
+  c.sfx = fu_turns_fixed(s * kInv2Pi);
+  c.fo_t = (f + oms) * kInv2Pi;
   c.st2 = 2. * s * kInv2Pi;
   c.nS[0] = ca * cd;
   c.nS[1] = sa * cd;
   c.nS[2] = sd;
+  for (int j = 0; j < 3; j++) c.nSf[j] = (float)c.nS[j];
   c.nD[0] = (R)(-ca * sd);
   c.nD[1] = (R)(-sa * sd);
   c.nD[2] = (R)cd;
@@ -156,18 +179,21 @@ __global__ void k_fu_select(FuCand<R>* __restrict__ cand, int n, const unsigned 
 template <typename R>
 struct Sample {
   R x, cm, sm;
+  float r0f, r1f, r2f;   // FP32 copy of the position (derivative factors)
   double r0, r1, r2;
+  double di;             // the sample index as FP64
 };
 
 // The phase of sample i for point c, returned as sin and cos in R.
 //   FP64 form: phi = f (i + shft) + (s i) i + (oms + 2 s i) shft
 //              (followup.c:460-462 order, no contraction)
-//   mixed:     the same in turns, reduced mod 1 in FP64, sin/cos of
-//              2 pi r in FP32 (sincospif).
+//   mixed:     phi/2pi = [f i + s i^2]/2pi + (f + oms + 2 s i) shft/2pi with
+//              the bracket in exact 64-bit fixed-point turns and the rest in
+//              FP64 reduced to fixed point; sin/cos of the top 32 bits in
+//              FP32 (sincospif).  Three FP64 operations besides shft.
 template <typename R>
-__device__ __forceinline__ void fu_phase(const FuCand<R>& c, double oms, double omt, int i, double shft, R* sn,
+__device__ __forceinline__ void fu_phase(const FuCand<R>& c, double oms, int i, double di, double shft, R* sn,
                                          R* cs) {
-  const double di = (double)i;
   if (sizeof(R) == 8) {
     const double phi = __dadd_rn(__dadd_rn(__dmul_rn(c.f, __dadd_rn(di, shft)), __dmul_rn(__dmul_rn(c.s, di), di)),
                                  __dmul_rn(__dadd_rn(oms, __dmul_rn(__dmul_rn(2., c.s), di)), shft));
@@ -176,11 +202,11 @@ __device__ __forceinline__ void fu_phase(const FuCand<R>& c, double oms, double 
     *sn = (R)s_;
     *cs = (R)c_;
   } else {
-    const double t2 = fma(c.st, di * di, c.ft * (di + shft));
-    const double t = fma(fma(c.st2, di, omt), shft, t2);
-    const float r = (float)(t - rint(t));
+    const unsigned long long ui = (unsigned long long)i;
+    const unsigned long long t =
+        c.ffx * ui + c.sfx * (ui * ui) + fu_turns_fixed(fma(c.st2, di, c.fo_t) * shft);
     float s_, c_;
-    sincospif(2.f * r, &s_, &c_);
+    sincospif((float)(int)(t >> 32) * 4.656612873077393e-10f, &s_, &c_);
     *sn = (R)s_;
     *cs = (R)c_;
   }
@@ -224,11 +250,14 @@ __global__ void __launch_bounds__(kThreads) k_fu_sums(const R* __restrict__ xd, 
     v.r0 = r[0];
     v.r1 = r[1];
     v.r2 = r[2];
+    v.r0f = (float)v.r0;
+    v.r1f = (float)v.r1;
+    v.r2f = (float)v.r2;
+    v.di = (double)i;
     sh[j] = v;
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const double omt = oms * kInv2Pi;
   const double is2 = dets.d[d].inv_sig2;
   const R k7 = (R)dets.d[d].amod[7], k8 = (R)dets.d[d].amod[8];
   for (int q = 0; q < kCandPerWarp; q++) {
@@ -253,7 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_fu_sums(const R* __restrict__ xd, 
       const R b = (R)2 * Q[7] * c2 + Q[8] * cs + Q[9] * cc + Q[10] * ss + Q[11];
       const double shft = c.nS[0] * v.r0 + c.nS[1] * v.r1 + c.nS[2] * v.r2;
       R sn, co;
-      fu_phase<R>(c, oms, omt, i, shft, &sn, &co);
+      fu_phase<R>(c, oms, i, v.di, shft, &sn, &co);
       if (!ADJ) {
         const R xa = v.x * a, xb = v.x * b;
         acc[0] += xa * co;
@@ -270,9 +299,13 @@ __global__ void __launch_bounds__(kThreads) k_fu_sums(const R* __restrict__ xd, 
         const R ga = v.x * c.ka * rea + (R)2 * c.qa * a;
         const R gb = v.x * c.kb * reb + (R)2 * c.qb * b;
         const R fi = (R)i;
-        const R sh_ = (R)shft;
-        const R sh_de = c.nD[0] * (R)v.r0 + c.nD[1] * (R)v.r1 + c.nD[2] * (R)v.r2;
-        const R sh_al = c.nA[0] * (R)v.r0 + c.nA[1] * (R)v.r1;
+        // derivative factors in the working precision (FP32 copies of the
+        // position in the mixed form: no per-sample conversions)
+        const R r0 = sizeof(R) == 4 ? (R)v.r0f : (R)v.r0, r1 = sizeof(R) == 4 ? (R)v.r1f : (R)v.r1,
+                r2 = sizeof(R) == 4 ? (R)v.r2f : (R)v.r2;
+        const R sh_ = sizeof(R) == 4 ? (R)(c.nSf[0] * v.r0f + c.nSf[1] * v.r1f + c.nSf[2] * v.r2f) : (R)shft;
+        const R sh_de = c.nD[0] * r0 + c.nD[1] * r1 + c.nD[2] * r2;
+        const R sh_al = c.nA[0] * r0 + c.nA[1] * r1;
         const R om = c.om0 + c.s2 * fi;
         // d a / d alpha, d b / d alpha
         const R a_al = -ss * ((R)4 * Q[2] * cc + Q[3] * ss + Q[4]) + cc * (Q[3] * cc + Q[5]);

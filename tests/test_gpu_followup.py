@@ -89,7 +89,7 @@ def test_adjoint_gradient_matches_fp64_oracle(form, fu_case, gpu_ok):
     _, gs = fu.fstatnet_grad(pts, seed=seed)
     want = w * grad * seed[:, None]
     rel = np.abs(w * gs - want).max(axis=1) / np.abs(want).max(axis=1)
-    assert rel.max() <= (1e-4 if form == "mixed" else 1e-12), rel
+    assert rel.max() <= (FORMS[form][2] if form == "mixed" else 1e-12), rel
 
 
 def test_adjoint_matches_finite_differences_fp64(fu_case, gpu_ok):
