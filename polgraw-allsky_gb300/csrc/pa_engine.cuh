@@ -496,18 +496,44 @@ __device__ __forceinline__ FF ff_axpy(FF a, FF x, FF y) {
 // can start kWarm steps early from zero: the start error shrinks by
 // 0.268^kWarm < 1e-18.  Chunks whose warm start reaches the array ends start
 // from the exact boundary values u_0 = 0, y2_{n-1} = 0.
-constexpr int kSplineChunk = 64;
-constexpr int kSplineWarm = 32;
-constexpr int kSplineChunks = 64;                          // recurrence threads per CTA
+// Chunking per form: the warm start must bring the start error below the
+// precision the result is stored in (y2 is stored in the working precision):
+// 0.268^16 = 7e-10 is far below FP32 rounding, 0.268^32 = 5e-19 below FP64's.
+// Shorter chunks in the FP32 forms also give twice the independent
+// recurrences, which these latency-bound sweeps need.
+template <typename R> struct SplineCfg;
+template <> struct SplineCfg<float> {
+  static constexpr int chunk = 32, warm = 16, log2chunk = 5;
+};
+template <> struct SplineCfg<double> {
+  static constexpr int chunk = 64, warm = 32, log2chunk = 6;
+};
 constexpr int kSplineThreads = 256;                        // threads for staging loads/stores
-constexpr int kSplineSeg = kSplineChunk * kSplineChunks;   // elements per CTA
+constexpr int kSplineSeg = 4096;                           // elements per CTA
+
+// Asynchronous global-to-shared copies (cp.async): every copy of a staging
+// loop is in flight at once, with no registers held; an invalid element is
+// zero-filled (source size 0, the source address is not read).
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 16 : 0)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gmem), "n"(BYTES),
+                 "r"(valid ? BYTES : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Shared-memory slot of staged element k: one padding element per chunk, so
-// that the recurrence threads (chunk starts kSplineChunk elements apart) hit
-// different banks.
-__device__ __forceinline__ int spad(int k) { return k + (k >> 6); }
-__host__ __device__ constexpr int spad_len(int n) { return n + (n >> 6) + 1; }
-static_assert(kSplineChunk == 64, "spad assumes 64-element chunks");
+// that the recurrence threads (chunk starts one chunk apart) hit different
+// banks.
+template <typename R>
+__device__ __forceinline__ int spad(int k) { return k + (k >> SplineCfg<R>::log2chunk); }
+template <typename R>
+__host__ __device__ constexpr int spad_len(int n) { return n + (n >> SplineCfg<R>::log2chunk) + 1; }
 
 // Forward sweep.  A CTA owns one segment of kSplineSeg elements of one
 // array; it stages y[seg - warm - 1, seg_end + 1) in shared memory with
@@ -520,41 +546,43 @@ __global__ void __launch_bounds__(kSplineThreads)
                  const double* __restrict__ invp) {
   typedef typename CT<R>::T T;
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  double2* us = reinterpret_cast<double2*>(sm_raw);                 // spad_len(kSplineSeg)
-  T* ys = reinterpret_cast<T*>(us + spad_len(kSplineSeg));          // spad_len(kSplineSeg + kSplineWarm + 2)
+  double2* us = reinterpret_cast<double2*>(sm_raw);                 // spad_len<R>(kSplineSeg)
+  T* ys = reinterpret_cast<T*>(us + spad_len<R>(kSplineSeg));          // spad_len<R>(kSplineSeg + SplineCfg<R>::warm + 2)
   const int q = blockIdx.x / nseg, sg = blockIdx.x - q * nseg;
   const T* yq = y + (size_t)q * ldy;
   double2* uq = u + (size_t)q * n;
   const int seg0 = sg * kSplineSeg;
-  const int y0 = seg0 - kSplineWarm - 1;                       // first staged index
-  const int ny = kSplineSeg + kSplineWarm + 2;
+  const int y0 = seg0 - SplineCfg<R>::warm - 1;                       // first staged index
+  const int ny = kSplineSeg + SplineCfg<R>::warm + 2;
   // the 64 pivots of the start of the array, in shared memory (the first
   // chunk's recurrence reads one per step)
   __shared__ double tab[64];
   if (threadIdx.x < 64) tab[threadIdx.x] = invp[threadIdx.x];
   for (int k = threadIdx.x; k < ny; k += kSplineThreads) {
     const int i = y0 + k;
-    ys[spad(k)] = (i >= 0 && i < n) ? yq[i] : mk((R)0, (R)0);
+    const bool ok = i >= 0 && i < n;
+    cp_async<(int)sizeof(T)>(&ys[spad<R>(k)], ok ? (const void*)(yq + i) : (const void*)yq, ok);
   }
+  cp_async_wait_all();
   __syncthreads();
-  if (threadIdx.x < kSplineChunks) {
-    const int lo = seg0 + threadIdx.x * kSplineChunk;
-    const int hi = min(lo + kSplineChunk, n - 1);
+  if (threadIdx.x < (kSplineSeg / SplineCfg<R>::chunk)) {
+    const int lo = seg0 + threadIdx.x * SplineCfg<R>::chunk;
+    const int hi = min(lo + SplineCfg<R>::chunk, n - 1);
     // u_i = (-u_{i-1}/2 + 3 d_i) invp_i = al_i u_{i-1} + be_i d_i; the
     // second difference d_i of the working-precision data is formed in that
     // precision (its rounding is below the data's own)
-    int i = max(1, lo - kSplineWarm);
-    T p = ys[spad(i - 1 - y0)], cc = ys[spad(i - y0)];
+    int i = max(1, lo - SplineCfg<R>::warm);
+    T p = ys[spad<R>(i - 1 - y0)], cc = ys[spad<R>(i - y0)];
     if (sizeof(R) == 8) {
       double ux = 0., uy = 0.;
       for (; i < hi; ++i) {
-        const T nn = ys[spad(i + 1 - y0)];
+        const T nn = ys[spad<R>(i + 1 - y0)];
         const R dx = p.x - (R)2 * cc.x + nn.x, dy = p.y - (R)2 * cc.y + nn.y;
         const int ti = i < 64 ? i : 63;
         const double al = -.5 * tab[ti], be = 3. * tab[ti];
         ux = fma(al, ux, be * (double)dx);
         uy = fma(al, uy, be * (double)dy);
-        if (i >= lo) us[spad(i - seg0)] = make_double2(ux, uy);
+        if (i >= lo) us[spad<R>(i - seg0)] = make_double2(ux, uy);
         p = cc;
         cc = nn;
       }
@@ -562,11 +590,11 @@ __global__ void __launch_bounds__(kSplineThreads)
       FF ux{0.f, 0.f}, uy{0.f, 0.f};
       float4* us4 = reinterpret_cast<float4*>(us);
       auto step = [&](FF al, float be) {
-        const T nn = ys[spad(i + 1 - y0)];
+        const T nn = ys[spad<R>(i + 1 - y0)];
         const float dx = (float)(p.x - (R)2 * cc.x + nn.x), dy = (float)(p.y - (R)2 * cc.y + nn.y);
         ux = ff_axpt(al, ux, __fmul_rn(be, dx));
         uy = ff_axpt(al, uy, __fmul_rn(be, dy));
-        if (i >= lo) us4[spad(i - seg0)] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
+        if (i >= lo) us4[spad<R>(i - seg0)] = make_float4(ux.hi, ux.lo, uy.hi, uy.lo);
         p = cc;
         cc = nn;
       };
@@ -578,11 +606,11 @@ __global__ void __launch_bounds__(kSplineThreads)
       const float be = (float)(3. * tab[63]);
       for (; i < hi; ++i) step(al, be);
     }
-    if (lo == 0) us[spad(0)] = make_double2(0., 0.);
+    if (lo == 0) us[spad<R>(0)] = make_double2(0., 0.);
   }
   __syncthreads();
   const int cnt = min(kSplineSeg, n - 1 - seg0);
-  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) uq[seg0 + k] = us[spad(k)];
+  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) uq[seg0 + k] = us[spad<R>(k)];
 }
 
 // Back substitution, same staging: u[seg0, seg_end + warm) in shared memory,
@@ -593,50 +621,51 @@ __global__ void __launch_bounds__(kSplineThreads)
                  const double* __restrict__ ptab) {
   typedef typename CT<R>::T T;
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  double2* us = reinterpret_cast<double2*>(sm_raw);                     // spad_len(kSplineSeg + kSplineWarm)
-  T* ys = reinterpret_cast<T*>(us + spad_len(kSplineSeg + kSplineWarm));  // spad_len(kSplineSeg)
+  double2* us = reinterpret_cast<double2*>(sm_raw);                     // spad_len<R>(kSplineSeg + SplineCfg<R>::warm)
+  T* ys = reinterpret_cast<T*>(us + spad_len<R>(kSplineSeg + SplineCfg<R>::warm));  // spad_len<R>(kSplineSeg)
   const int q = blockIdx.x / nseg, sg = blockIdx.x - q * nseg;
   const double2* uq = u + (size_t)q * n;
   T* yq = y2 + (size_t)q * n;
   const int seg0 = sg * kSplineSeg;
-  const int nu = min(kSplineSeg + kSplineWarm, n - 1 - seg0);  // u defined on [0, n-2]
+  const int nu = min(kSplineSeg + SplineCfg<R>::warm, n - 1 - seg0);  // u defined on [0, n-2]
   __shared__ double tab[64];
   if (threadIdx.x < 64) tab[threadIdx.x] = ptab[threadIdx.x];
-  for (int k = threadIdx.x; k < nu; k += kSplineThreads) us[spad(k)] = uq[seg0 + k];
+  for (int k = threadIdx.x; k < nu; k += kSplineThreads) cp_async<16>(&us[spad<R>(k)], uq + seg0 + k, true);
+  cp_async_wait_all();
   __syncthreads();
-  const int lo = seg0 + threadIdx.x * kSplineChunk;
-  const int hi = min(lo + kSplineChunk, n);
-  if (threadIdx.x < kSplineChunks && lo < n) {
-    const int kst = min(n - 2, hi - 1 + kSplineWarm);
+  const int lo = seg0 + threadIdx.x * SplineCfg<R>::chunk;
+  const int hi = min(lo + SplineCfg<R>::chunk, n);
+  if (threadIdx.x < (kSplineSeg / SplineCfg<R>::chunk) && lo < n) {
+    const int kst = min(n - 2, hi - 1 + SplineCfg<R>::warm);
     if (sizeof(R) == 8) {
       double vx = 0., vy = 0.;
       for (int k = kst; k >= lo; --k) {
         const double p = tab[k < 64 ? k : 63];
-        const double2 uk = us[spad(k - seg0)];
+        const double2 uk = us[spad<R>(k - seg0)];
         vx = p * vx + uk.x;
         vy = p * vy + uk.y;
-        if (k < hi) ys[spad(k - seg0)] = mk((R)vx, (R)vy);
+        if (k < hi) ys[spad<R>(k - seg0)] = mk((R)vx, (R)vy);
       }
     } else {
       const float4* us4 = reinterpret_cast<const float4*>(us);
       FF vx{0.f, 0.f}, vy{0.f, 0.f};
       int k = kst;
       auto step = [&](FF pc) {
-        const float4 uk = us4[spad(k - seg0)];
+        const float4 uk = us4[spad<R>(k - seg0)];
         vx = ff_axpy(pc, vx, FF{uk.x, uk.y});
         vy = ff_axpy(pc, vy, FF{uk.z, uk.w});
-        if (k < hi) ys[spad(k - seg0)] = mk((R)vx.hi, (R)vy.hi);
+        if (k < hi) ys[spad<R>(k - seg0)] = mk((R)vx.hi, (R)vy.hi);
       };
       // constant coefficient down to k = 64, then the table
       const FF pc63 = ff_split(tab[63]);
       for (; k >= lo && k >= 64; --k) step(pc63);
       for (; k >= lo; --k) step(ff_split(tab[k]));
     }
-    if (hi == n) ys[spad(n - 1 - seg0)] = mk((R)0, (R)0);
+    if (hi == n) ys[spad<R>(n - 1 - seg0)] = mk((R)0, (R)0);
   }
   __syncthreads();
   const int cnt = min(kSplineSeg, n - seg0);
-  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) yq[seg0 + k] = ys[spad(k)];
+  for (int k = threadIdx.x; k < cnt; k += kSplineThreads) yq[seg0 + k] = ys[spad<R>(k)];
 }
 
 // splint at x = interpftpad (i - shftf_i) (auxi.c:83-122), then / sig2
@@ -977,9 +1006,9 @@ template <typename R, int PM> class EngineT : public Engine {
     // spline through the first 2N points of each resampled array
     const int n = 2 * N;
     const int nseg = (n + kSplineSeg - 1) / kSplineSeg;
-    const int smf = spad_len(kSplineSeg) * (int)sizeof(double2) +
-                    spad_len(kSplineSeg + kSplineWarm + 2) * (int)sizeof(T);
-    const int smb = spad_len(kSplineSeg + kSplineWarm) * (int)sizeof(double2) + spad_len(kSplineSeg) * (int)sizeof(T);
+    constexpr int W = SplineCfg<R>::warm;
+    const int smf = spad_len<R>(kSplineSeg) * (int)sizeof(double2) + spad_len<R>(kSplineSeg + W + 2) * (int)sizeof(T);
+    const int smb = spad_len<R>(kSplineSeg + W) * (int)sizeof(double2) + spad_len<R>(kSplineSeg) * (int)sizeof(T);
     static bool donef = false, doneb = false;
     smem_attr(k_spline_fwd<R>, smf, donef);
     smem_attr(k_spline_bwd<R>, smb, doneb);
