@@ -554,10 +554,20 @@ __global__ void __launch_bounds__(kSplineThreads)
   const int seg0 = sg * kSplineSeg;
   const int y0 = seg0 - SplineCfg<R>::warm - 1;                       // first staged index
   const int ny = kSplineSeg + SplineCfg<R>::warm + 2;
-  // the 64 pivots of the start of the array, in shared memory (the first
-  // chunk's recurrence reads one per step)
+  // the coefficients of the first 64 steps of the array, in shared memory
+  // (the first chunks' recurrences read one per step): FP64 pivots for the
+  // FP64 form, their float-float splits (formed here in parallel, keeping
+  // FP64 work out of the sequential recurrence) for the FP32 forms
   __shared__ double tab[64];
-  if (threadIdx.x < 64) tab[threadIdx.x] = invp[threadIdx.x];
+  __shared__ float tal_h[64], tal_l[64], tbe[64];
+  if (threadIdx.x < 64) {
+    const double v = invp[threadIdx.x];
+    tab[threadIdx.x] = v;
+    const FF a = ff_split(-.5 * v);
+    tal_h[threadIdx.x] = a.hi;
+    tal_l[threadIdx.x] = a.lo;
+    tbe[threadIdx.x] = (float)(3. * v);
+  }
   for (int k = threadIdx.x; k < ny; k += kSplineThreads) {
     const int i = y0 + k;
     const bool ok = i >= 0 && i < n;
@@ -601,9 +611,9 @@ __global__ void __launch_bounds__(kSplineThreads)
       // the first 63 steps of the array have their own coefficients; from
       // i = 63 on they are constant (two loops keep the FP64 table reads out
       // of the main one)
-      for (; i < hi && i < 63; ++i) step(ff_split(-.5 * tab[i]), (float)(3. * tab[i]));
-      const FF al = ff_split(-.5 * tab[63]);
-      const float be = (float)(3. * tab[63]);
+      for (; i < hi && i < 63; ++i) step(FF{tal_h[i], tal_l[i]}, tbe[i]);
+      const FF al{tal_h[63], tal_l[63]};
+      const float be = tbe[63];
       for (; i < hi; ++i) step(al, be);
     }
     if (lo == 0) us[spad<R>(0)] = make_double2(0., 0.);
@@ -629,7 +639,14 @@ __global__ void __launch_bounds__(kSplineThreads)
   const int seg0 = sg * kSplineSeg;
   const int nu = min(kSplineSeg + SplineCfg<R>::warm, n - 1 - seg0);  // u defined on [0, n-2]
   __shared__ double tab[64];
-  if (threadIdx.x < 64) tab[threadIdx.x] = ptab[threadIdx.x];
+  __shared__ float tp_h[64], tp_l[64];
+  if (threadIdx.x < 64) {
+    const double v = ptab[threadIdx.x];
+    tab[threadIdx.x] = v;
+    const FF a = ff_split(v);
+    tp_h[threadIdx.x] = a.hi;
+    tp_l[threadIdx.x] = a.lo;
+  }
   for (int k = threadIdx.x; k < nu; k += kSplineThreads) cp_async<16>(&us[spad<R>(k)], uq + seg0 + k, true);
   cp_async_wait_all();
   __syncthreads();
@@ -657,9 +674,9 @@ __global__ void __launch_bounds__(kSplineThreads)
         if (k < hi) ys[spad<R>(k - seg0)] = mk((R)vx.hi, (R)vy.hi);
       };
       // constant coefficient down to k = 64, then the table
-      const FF pc63 = ff_split(tab[63]);
+      const FF pc63{tp_h[63], tp_l[63]};
       for (; k >= lo && k >= 64; --k) step(pc63);
-      for (; k >= lo; --k) step(ff_split(tab[k]));
+      for (; k >= lo; --k) step(FF{tp_h[k], tp_l[k]});
     }
     if (hi == n) ys[spad<R>(n - 1 - seg0)] = mk((R)0, (R)0);
   }
