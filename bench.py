@@ -466,11 +466,19 @@ def main():
         print(json.dumps(line))
         return
 
+    # N > 1: one replica of the whole workload per GPU (sky points are
+    # independent, nothing is exchanged); the step time is the maximum over
+    # ranks and the work the sum (weak scaling)
+    from polgraw_gb300 import replicas
+    replicas.init()
+    local = replicas.world()[2]
+    device = local if world > 1 else 0
     if world > 1:
-        tasks = tasks[rank::world]
+        import torch
+        torch.cuda.set_device(device)
     dets, nifo = host.detectors()
     phase = L.PHASE_NAMES[args.phase]
-    ctx = L.Context(s, dets, nifo, precision=L.PA_PREC_MIXED, phase_mode=phase, device=0)
+    ctx = L.Context(s, dets, nifo, precision=L.PA_PREC_MIXED, phase_mode=phase, device=device)
     opts, rng = host.opts(), host.range
     templates = len(tasks) * nspin * bins
     if args.schedule:
@@ -483,7 +491,8 @@ def main():
     for _ in range(args.warmup):
         ctx.search_batch(tasks, opts, rng)
     launches0 = ctx.launches()
-    clocks = ClockSampler(0)
+    replicas.barrier()
+    clocks = ClockSampler(device)
     dev_ms = []
     ncand = 0
     for _ in range(args.steps):
@@ -491,20 +500,23 @@ def main():
         rec, idx, fnum = ctx.search_batch(tasks, opts, rng)
         dev_ms.append(ctx.last_call_ms())
         ncand = len(rec)
+    replicas.barrier()
     clk = clocks.stop()
     launches = (ctx.launches() - launches0) // max(1, args.steps)
-    t_dev = sum(dev_ms) / 1e3
-    value = templates * args.steps / t_dev
+    t_dev, templates_all = replicas.reduce_step(sum(dev_ms) / 1e3, float(templates))
+    value = templates_all * args.steps / t_dev
 
     # end to end: host buffers in, candidates out, through the C-ABI
     e2e_t = 0.0
+    replicas.barrier()
     for _ in range(args.steps):
         l2_flush()
         t0 = time.perf_counter()
         ctx.set_data(dets, nifo)
         rec, idx, fnum = ctx.search_batch(tasks, opts, rng)
         e2e_t += time.perf_counter() - t0
-    e2e = templates * args.steps / e2e_t
+    e2e_t, _ = replicas.reduce_step(e2e_t, 0.0)
+    e2e = templates_all * args.steps / e2e_t
     h2d = nifo * s.N * 8 * 4
     d2h = 4 + len(rec) * 24
 
@@ -517,7 +529,7 @@ def main():
            "schedule": {"spindown_batch": sched[0], "fft_split": sched[1],
                         "autotuned": bool(args.autotune) and not args.schedule}}
 
-    if not args.no_extras:
+    if not args.no_extras and rank == 0:
         # per-kernel CUDA-event profile of one step (not the timed number)
         ctx.set_profiling(True)
         ctx.profile_reset()
@@ -588,6 +600,7 @@ def main():
     if rank == 0:
         print(json.dumps(out))
     ctx.close()
+    replicas.shutdown()
 
 
 if __name__ == "__main__":

@@ -47,7 +47,7 @@ struct pa_ctx {
   cudaEvent_t ev_pre[2] = {nullptr, nullptr}, ev_spin[2] = {nullptr, nullptr};
   pa::Buffers b;
   std::vector<void*> allocs;
-  Twiddles tw_fwd, tw_inv, tw_main;
+  Twiddles tw_fwd, tw_inv, tw_invh, tw_main;
   pa::Engine* eng = nullptr;
   pa::DevCand* h_cand = nullptr;  // pinned
   int* h_ncand = nullptr;          // pinned
@@ -316,10 +316,12 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   CK(cudaMemcpy((void*)b.spline_p, p, sizeof(p), cudaMemcpyHostToDevice), "upload spline");
   if ((rc = make_twiddles(c, s.nfft, -1, &c->tw_fwd))) return rc;
   if ((rc = make_twiddles(c, s.Ninterp, +1, &c->tw_inv))) return rc;
+  if ((rc = make_twiddles(c, s.nfft, +1, &c->tw_invh))) return rc;
   if ((rc = make_twiddles(c, s.nfftf, -1, &c->tw_main))) return rc;
   for (int k = 0; k < 4; k++) {
     b.tw_fwd[k] = c->tw_fwd.p[k];
     b.tw_inv[k] = c->tw_inv.p[k];
+    b.tw_invh[k] = c->tw_invh.p[k];
     b.tw_main[k] = c->tw_main.p[k];
   }
   if ((rc = upload_data(c, det))) return rc;
@@ -1057,7 +1059,7 @@ int noalloc_fail(int code, const char* fmt, ...) {
 
 // Lays the buffers of one search out in the scratch (or only sizes them
 // when base == nullptr); returns the bytes used.
-size_t noalloc_layout(char* base, const pa_settings& s, int nifo, pa::Buffers* b, void* tw[3][4], void** Fn) {
+size_t noalloc_layout(char* base, const pa_settings& s, int nifo, pa::Buffers* b, void* tw[4][4], void** Fn) {
   Bump m{base};
   const size_t N = s.N, cs = 8;
   const int bins = s.nmax - s.nmin;
@@ -1087,8 +1089,8 @@ size_t noalloc_layout(char* base, const pa_settings& s, int nifo, pa::Buffers* b
   *Fn = m.take(4 * (size_t)bins);  // normalised F (the output)
   b->cand = (pa::DevCand*)m.take(sizeof(pa::DevCand) * kNoAllocCandCap);
   b->ncand = (int*)m.take(16);
-  const int lens[3] = {s.nfft, s.Ninterp, s.nfftf};
-  for (int t = 0; t < 3; t++) {
+  const int lens[4] = {s.nfft, s.Ninterp, s.nfftf, s.nfft};
+  for (int t = 0; t < 4; t++) {
     int lg = 0;
     while ((1 << lg) < lens[t]) ++lg;
     const int n4[4] = {1 << ((lg + 1) / 2), 1 << (lg / 2), 1024, lens[t] / 1024};
@@ -1110,6 +1112,7 @@ size_t noalloc_layout(char* base, const pa_settings& s, int nifo, pa::Buffers* b
     b->tw_fwd[k] = tw[0][k];
     b->tw_inv[k] = tw[1][k];
     b->tw_main[k] = tw[2][k];
+    b->tw_invh[k] = tw[3][k];
   }
   return m.off;
 }
@@ -1165,7 +1168,7 @@ extern "C" int pa_fstat_noalloc(const pa_settings* sett, const pa_detector* det,
   if (device < 0 || device >= kNoAllocMaxDevices || device >= pa_device_count())
     return noalloc_fail(PA_ERR_NODEV, "pa_fstat_noalloc: no CUDA device %d", device);
   pa::Buffers b;
-  void* tw[3][4];
+  void* tw[4][4];
   void* Fn = nullptr;
   const size_t need = noalloc_layout(nullptr, *sett, nifo, &b, tw, &Fn);
   if (need > kNoAllocBytes)
@@ -1231,6 +1234,7 @@ extern "C" int pa_fstat_noalloc(const pa_settings* sett, const pa_detector* det,
   NCK(noalloc_twiddles(sett->nfft, -1, tw[0], st), "twiddles");
   NCK(noalloc_twiddles(sett->Ninterp, +1, tw[1], st), "twiddles");
   NCK(noalloc_twiddles(sett->nfftf, -1, tw[2], st), "twiddles");
+  NCK(noalloc_twiddles(sett->nfft, +1, tw[3], st), "twiddles");
   // what must start at zero
   NCK(cudaMemsetAsync(b.counter, 0, 16, st), "memset");
   NCK(cudaMemsetAsync(b.ncand, 0, 16, st), "memset");

@@ -5,7 +5,9 @@
 // Reference correspondence (search/network/src-cpu):
 //   k_prelude_mod   modvir (settings.c:281-325), shft/shftf/_tmp1 and the
 //                   prelude phase modulation (jobcore.c:277-313)
-//   resample FFTs   jobcore.c:319-362 (pass A/B with PlainLoader, RemapLoader)
+//   resample FFTs   jobcore.c:319-362 (pass A/B with PlainLoader; the
+//                   interpolating inverse at half length: HalfShiftLoader,
+//                   InterpStore)
 //   k_spline_fwd/bwd spline() (auxi.c:56-81), FP64 chunked recurrences
 //   k_splint        splint/splintpad (auxi.c:83-122) + 1/sig2 (jobcore.c:386-389)
 //   k_prelude_sums  aa, bb (jobcore.c:375-393)
@@ -265,21 +267,28 @@ template <typename R> struct PlainLoader {
   }
 };
 
-// Spectrum remap of jobcore.c:338-352: bins [0, nyqst) stay, [nyqst, nfft)
-// move up by Ninterp - nfft, the gap is zero.
-template <typename R> struct RemapLoader {
+// The interpolating inverse transform of jobcore.c:338-362 at half length.
+// The reference keeps bins [0, nyqst) of the length-nfft spectrum X, moves
+// [nyqst, nfft) up by Ninterp - nfft = nfft and inverse-transforms at length
+// Ninterp = 2 nfft with scale 2/Ninterp.  With that remap the output is
+//   y[2m]   = x[m]                                  (the input itself)
+//   y[2m+1] = (1/nfft) sum_j X[j] s_j e^{i pi j/nfft} e^{2 pi i j m/nfft}
+// with s_j = +1 below nyqst and -1 from it (the moved bins pick up
+// e^{i pi (2m+1)} = -1), i.e. an inverse FFT of length nfft of the
+// phase-shifted spectrum: half the transform length, and no transform of the
+// zero gap.  This loader feeds that transform; InterpStore interleaves.
+template <typename R> struct HalfShiftLoader {
   typedef typename CT<R>::T T;
-  const T* spec;   // [batch][2][nfft]
-  int nfft, nyqst, shift;
+  const T* spec;    // [batch][2][nfft]
+  const T* twlo;    // e^{+2 pi i m/Ninterp}, m < 1024
+  const T* twhi;    // e^{+2 pi i 1024 m/Ninterp}
+  int nfft, nyqst;
   __device__ __forceinline__ void prologue(int, char*) const {}
   __device__ __forceinline__ void load2(int batch, int j, T& a, T& b, const char*) const {
-    int idx = j < nyqst ? j : (j < nyqst + shift ? -1 : j - shift);
-    if (idx >= 0) {
-      a = spec[((size_t)batch * 2 + 0) * nfft + idx];
-      b = spec[((size_t)batch * 2 + 1) * nfft + idx];
-    } else {
-      a = b = mk((R)0, (R)0);
-    }
+    const T w0 = cmul(__ldg(&twlo[j & 1023]), __ldg(&twhi[j >> 10]));
+    const T w = j < nyqst ? w0 : mk(-w0.x, -w0.y);
+    a = cmul(spec[((size_t)batch * 2 + 0) * nfft + j], w);
+    b = cmul(spec[((size_t)batch * 2 + 1) * nfft + j], w);
   }
 };
 
@@ -439,6 +448,26 @@ template <typename R> struct FstatStore {
       const R ia = __ldg(&inv[0]), ib = __ldg(&inv[1]);
       F[(size_t)batch * bins + (k - nmin)] = (a.x * a.x + a.y * a.y) * ia + (b.x * b.x + b.y * b.y) * ib;
     }
+  }
+};
+
+// Output of the half-length interpolating transform: y[2m] = x[m] (zero
+// past the N input samples), y[2m+1] = transform[m] / nfft, written as one
+// 16-byte pair per (array, m) into yint [batch][2][Ninterp].
+template <typename R> struct InterpStore {
+  typedef typename CT<R>::T T;
+  T* yint;
+  const T* xin;     // [batch][2][N]
+  int N, Ninterp;
+  R scale;          // 1/nfft
+  __device__ __forceinline__ void begin(int, int) const {}
+  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, int logL1) const {
+    const int m = k1 + (k2 << logL1);
+    const size_t qa = (size_t)batch * 2, qb = qa + 1;
+    const T xa = m < N ? xin[qa * N + m] : mk((R)0, (R)0);
+    const T xb = m < N ? xin[qb * N + m] : mk((R)0, (R)0);
+    Pair<T>::st(yint + qa * Ninterp + 2 * (size_t)m, xa, mk(a.x * scale, a.y * scale));
+    Pair<T>::st(yint + qb * Ninterp + 2 * (size_t)m, xb, mk(b.x * scale, b.y * scale));
   }
 };
 
@@ -912,7 +941,7 @@ inline Geom make_geom(int L, int E) {
 template <typename R, int PM> class EngineT : public Engine {
   typedef typename CT<R>::T T;
   Buffers b_;
-  Geom gf_, gi_, gm_;
+  Geom gf_, gm_;
   long long launches_ = 0;
   int split_ = 0;
 
@@ -991,7 +1020,6 @@ template <typename R, int PM> class EngineT : public Engine {
  public:
   explicit EngineT(const Buffers& b) : b_(b) {
     gf_ = make_geom(b.nfft, TileCfg<R>::E);
-    gi_ = make_geom(b.Ninterp, TileCfg<R>::E);
     gm_ = make_geom(b.nfftf, TileCfg<R>::E);
   }
 
@@ -1015,10 +1043,12 @@ template <typename R, int PM> class EngineT : public Engine {
     CStore<R> cs1{(T*)b_.spec, b_.nfft, (R)1};
     cudaError_t e = fft<-1>(gf_, b_.tw_fwd, pl, cs1, nifo, st, KK_FFT_FWD_A, KK_FFT_FWD_B, b_.ybuf_pre);
     if (e != cudaSuccess) return e;
-    // spectrum remap + backward FFT (length Ninterp), scale interpftpad/Ninterp
-    RemapLoader<R> rl{(const T*)b_.spec, b_.nfft, b_.nfft / 2 + 1, b_.Ninterp - b_.nfft};
-    CStore<R> cs2{(T*)b_.yint, b_.Ninterp, (R)(2.0 / b_.Ninterp)};
-    e = fft<+1>(gi_, b_.tw_inv, rl, cs2, nifo, st, KK_FFT_INV_A, KK_FFT_INV_B, b_.ybuf_pre);
+    // spectrum remap + backward FFT of length Ninterp, scale interpftpad/Ninterp
+    // (jobcore.c:338-362), as a half-length transform (HalfShiftLoader)
+    HalfShiftLoader<R> hl{(const T*)b_.spec, (const T*)b_.tw_inv[2], (const T*)b_.tw_inv[3], b_.nfft,
+                          b_.nfft / 2 + 1};
+    InterpStore<R> is{(T*)b_.yint, (const T*)b_.xin, N, b_.Ninterp, (R)(1.0 / b_.nfft)};
+    e = fft<+1>(gf_, b_.tw_invh, hl, is, nifo, st, KK_FFT_INV_A, KK_FFT_INV_B, b_.ybuf_pre);
     if (e != cudaSuccess) return e;
     // spline through the first 2N points of each resampled array
     const int n = 2 * N;

@@ -85,7 +85,8 @@ struct Buffers {
   int cand_cap;
   // twiddle tables (Real complex) per transform
   const void* tw_fwd[4];            // nfft forward: tw1, tw2, twlo, twhi
-  const void* tw_inv[4];            // Ninterp backward
+  const void* tw_inv[4];            // Ninterp backward (its twlo/twhi give e^{+i pi j/nfft})
+  const void* tw_invh[4];           // nfft backward (the half-length resampling transform)
   const void* tw_main[4];           // nfftf forward
 };
 
