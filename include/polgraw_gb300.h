@@ -239,9 +239,10 @@ int pa_set_graphs(pa_ctx *ctx, int on);
 int pa_set_schedule(pa_ctx *ctx, int sbatch, int split);
 int pa_get_schedule(const pa_ctx *ctx, int *sbatch, int *split, int *max_sbatch);
 
-/* Times the candidate schedules (three spindown batches x the possible
- * splits) on the given sky points (each searched three times, the first as
- * warm-up, CUDA-event device time) and keeps the fastest; returns it in
+/* Times the candidate schedules (four spindown batches, 1/4 .. 4/4 of the
+ * maximum, x the possible splits) on the given sky points (each searched
+ * three times, the first as warm-up, CUDA-event device time) and keeps the
+ * fastest; returns it in
  * *sbatch, *split (either may be NULL).  Results do not depend on sbatch;
  * the split changes FFT rounding only. */
 int pa_autotune(pa_ctx *ctx, const pa_sky *tasks, int ntasks, const pa_opts *opts, const pa_range *s_range,

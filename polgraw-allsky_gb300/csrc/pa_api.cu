@@ -66,10 +66,10 @@ struct pa_ctx {
 
 namespace pa {
 const char* kernel_kind_name(int k) {
-  static const char* names[KK_COUNT] = {"prelude_mod", "prelude_sums", "resample_fft_fwd_a",
-                                        "resample_fft_fwd_b", "resample_fft_inv_a", "resample_fft_inv_b",
-                                        "spline_fwd", "spline_bwd", "splint", "spindown_pass_a",
-                                        "spindown_pass_b_fstat", "fstat_blockmean", "threshold"};
+  static const char* names[KK_COUNT] = {"prelude_mod", "resample_fft_fwd_a", "resample_fft_fwd_b",
+                                        "resample_fft_inv_a", "resample_fft_inv_b", "spline_fwd",
+                                        "spline_bwd", "splint", "spindown_pass_a", "spindown_pass_b_fstat",
+                                        "threshold"};
   return (k >= 0 && k < KK_COUNT) ? names[k] : "";
 }
 }  // namespace pa
@@ -881,13 +881,14 @@ int pa_autotune(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o, co
   for (int t = 0; t < ntasks; t++)
     sky_setup(c, tasks[t].pm, tasks[t].mm, tasks[t].nn, o, t == 0 ? r->sst : r->spndr[0], r->spndr[1], &hs[t]);
   const int sb0 = c->b.sbatch, sp0 = c->eng->split();
-  int cands[3] = {std::max(1, c->sb_max / 4), std::max(1, c->sb_max / 2), c->sb_max};
+  int cands[4] = {std::max(1, c->sb_max / 4), std::max(1, c->sb_max / 2), std::max(1, 3 * c->sb_max / 4),
+                  c->sb_max};
   // the factor split is a choice only for odd log2(nfftf)
   const int nsplit = (c->sett.nfftf & 0xAAAAAAAA) ? 2 : 1;
   double best = 1e300;
   int bsb = sb0, bsp = sp0;
   std::vector<pa::DevCand> out;
-  for (int k = 0; k < 3; k++) {
+  for (int k = 0; k < 4; k++) {
     if (k > 0 && cands[k] == cands[k - 1]) continue;
     for (int sp = 0; sp < nsplit; sp++) {
       c->b.sbatch = cands[k];

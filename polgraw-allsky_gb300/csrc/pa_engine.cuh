@@ -10,11 +10,11 @@
 //                   InterpStore)
 //   k_spline_fwd/bwd spline() (auxi.c:56-81), FP64 chunked recurrences
 //   k_splint        splint/splintpad (auxi.c:83-122) + 1/sig2 (jobcore.c:386-389)
-//   k_prelude_sums  aa, bb (jobcore.c:375-393)
+//   (aa, bb: last-CTA reduction of k_prelude_mod, jobcore.c:375-393)
 //   SpinLoader      spindown phase modulation (jobcore.c:455-623)
 //   FstatStore      F = |Xa|^2/aa + |Xb|^2/bb (jobcore.c:635-638)
-//   k_blockmean     FStat() block means (auxi.c:214-240)
-//   k_threshold     threshold, run clustering, argmax (jobcore.c:659-669)
+//   k_normthresh    FStat() block means and normalisation (auxi.c:214-240),
+//                   threshold, run clustering, argmax (jobcore.c:659-669)
 #pragma once
 #include <math.h>
 #include <stdint.h>
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(256)
                   const R* __restrict__ cosmodf, const R* __restrict__ sinmodf,
                   const DetConst* __restrict__ dc, const SkyArgs sky, int N,
                   typename CT<R>::T* __restrict__ xin, double* __restrict__ shftf, void* ph0,
-                  void* ph1, double* __restrict__ part, double* __restrict__ sums, R* __restrict__ sums_r,
+                  double* __restrict__ part, double* __restrict__ sums, R* __restrict__ sums_r,
                   unsigned int* __restrict__ counter) {
   typedef typename CT<R>::T T;
   const int d = blockIdx.y;
@@ -1034,7 +1034,7 @@ template <typename R, int PM> class EngineT : public Engine {
     pre(KK_PRELUDE_MOD, nifo, st);
     k_prelude_mod<R, PM><<<dim3(nbx, nifo), 256, 0, st>>>(
         b_.xDat, b_.DetSSB, (const R*)b_.cosmodf, (const R*)b_.sinmodf, b_.dc, sky, N, (T*)b_.xin,
-        b_.shftf, sizeof(R) == 8 ? b_.ph0[slot] : b_.xm[slot], nullptr, b_.part, b_.sums[slot],
+        b_.shftf, sizeof(R) == 8 ? b_.ph0[slot] : b_.xm[slot], b_.part, b_.sums[slot],
         (R*)b_.sums_r[slot], b_.counter);
     post(st);
     launches_ += 1;

@@ -68,7 +68,6 @@ struct Buffers {
   // of one sky point runs while the spindowns of the previous one read the
   // other slot
   void* ph0[2];                     // FP64 form: tmp1 [nifo][N]
-  void* ph1[2];                     // (unused)
   void* xm[2];                      // FP32 forms: [nifo][N] 32-byte records
                                     // {xa, xb | phase terms}; FP64 form:
                                     // [nifo][2][N] double complex
@@ -92,8 +91,8 @@ struct Buffers {
 
 // Kernel kinds for the optional per-launch CUDA-event profile.
 enum KernelKind {
-  KK_PRELUDE_MOD = 0, KK_PRELUDE_SUMS, KK_FFT_FWD_A, KK_FFT_FWD_B, KK_FFT_INV_A, KK_FFT_INV_B,
-  KK_SPLINE_FWD, KK_SPLINE_BWD, KK_SPLINT, KK_SPIN_A, KK_SPIN_B, KK_BLOCKMEAN, KK_THRESHOLD, KK_COUNT
+  KK_PRELUDE_MOD = 0, KK_FFT_FWD_A, KK_FFT_FWD_B, KK_FFT_INV_A, KK_FFT_INV_B, KK_SPLINE_FWD, KK_SPLINE_BWD,
+  KK_SPLINT, KK_SPIN_A, KK_SPIN_B, KK_THRESHOLD, KK_COUNT
 };
 const char* kernel_kind_name(int k);
 
@@ -137,12 +136,5 @@ Engine* make_engine_f32(const Buffers& b, int phase_mode);
 Engine* make_engine_f32_fixed_at(void* mem, size_t bytes, const Buffers& b);
 Engine* make_engine_f64(const Buffers& b);
 
-// Phase-coefficient bytes per sample for a (precision, phase mode).
-inline size_t phase_bytes(int fp64, int phase_mode, int which) {
-  if (fp64) return which == 0 ? 8 : 0;
-  if (phase_mode == 1) return 8;          // fixed: A and B (u64 each)
-  if (phase_mode == 2) return which == 0 ? 8 : 0;  // float-float
-  return which == 0 ? 8 : 0;              // FP64 tmp1
-}
 
 }  // namespace pa
