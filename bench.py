@@ -586,6 +586,11 @@ def main():
             out["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": nth, "kind": "port",
                                    "sample": "%d sky points x %d spindowns (CPU oracle, OpenMP, %.1f s)" %
                                              (cn, nspin, cdt)}
+            # and the serial form on one core (the reference's src-cpu build)
+            c1v, c1dt, c1n = cpu_baseline(host, tasks, 1, 1)
+            out["cpu_baseline_1core"] = {"value": c1v, "unit": UNIT, "cores": 1, "kind": "port",
+                                         "sample": "1 sky point x %d spindowns (CPU oracle, one thread, %.1f s)" %
+                                                   (nspin, c1dt)}
             # relative F-statistic error of the mixed form against the FP64 CPU oracle
             rg, ig, _ = ctx.search_batch(tasks[:cn], opts, rng)
             got = {tuple(int(x[f]) for f in ("pm", "mm", "nn", "ss", "ii")): r[4] * r[4] / 2 + 2

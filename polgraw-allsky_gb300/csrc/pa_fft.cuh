@@ -239,13 +239,17 @@ __device__ __forceinline__ void fft_front(T* s, const T* tw, const Src& src) {
 
 // Per-precision tile configuration.
 template <typename R> struct TileCfg;
+// (4096-element FP32 tiles with 256 threads and 4 CTAs per SM were measured
+// 1% slower on the spindown passes)
 template <> struct TileCfg<float> {
   static constexpr int E = 8192;   // complex elements per tile (64 KB)
   static constexpr int NT = 512;   // threads per CTA
+  static constexpr int MINB = 2;   // resident CTAs per SM the registers are sized for
 };
 template <> struct TileCfg<double> {
   static constexpr int E = 4096;   // 64 KB
   static constexpr int NT = 256;
+  static constexpr int MINB = 2;
 };
 
 template <typename R> __host__ __device__ constexpr int tile_pitch(int Cs) {
@@ -258,7 +262,7 @@ template <typename R> __host__ __device__ constexpr int tile_pitch(int Cs) {
 // radix schedules of the passes swap with them).
 template <typename R, int LOGL, int SPLIT = 0> struct FftShape {
   static constexpr int E = TileCfg<R>::E, NT = TileCfg<R>::NT;
-  static constexpr int logE = E == 8192 ? 13 : 12;
+  static constexpr int logE = E == 8192 ? 13 : (E == 4096 ? 12 : 11);
   static constexpr int LOGL1 = SPLIT ? LOGL / 2 : (LOGL + 1) / 2, LOGL2 = LOGL - LOGL1;
   static constexpr int L1 = 1 << LOGL1, L2 = 1 << LOGL2;
   static constexpr int LOGC = logE - 1 - LOGL1, C = 1 << LOGC;      // pass-A columns per tile
@@ -276,7 +280,7 @@ template <typename R, int LOGL, int SPLIT = 0> struct FftShape {
 // global memory, 16 contiguous bytes per lane.
 // Loader: prologue(batch, smem scratch) and load2(batch, n, a, b, scratch).
 template <typename R, int SIGN, int LOGL, class Loader, int SPLIT = 0>
-__global__ void __launch_bounds__(TileCfg<R>::NT, 2)
+__global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
     k_pass_a(const Loader ld, const typename CT<R>::T* __restrict__ tw1,
              const typename CT<R>::T* __restrict__ twlo, const typename CT<R>::T* __restrict__ twhi,
              typename CT<R>::T* __restrict__ ybuf) {
@@ -322,7 +326,7 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, 2)
 //   __device__ void put(int batch, int k1, int k2, T a, T b, int logL1) const
 // with consecutive lanes on consecutive k1.
 template <typename R, int SIGN, int LOGL, class Storer, int SPLIT = 0>
-__global__ void __launch_bounds__(TileCfg<R>::NT, 2)
+__global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
     k_pass_b(const Storer st, const typename CT<R>::T* __restrict__ tw2,
              const typename CT<R>::T* __restrict__ ybuf) {
   typedef typename CT<R>::T T;
