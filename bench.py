@@ -224,7 +224,7 @@ def run_stress(args, L):
             "forms": summary, "oracle_sample": "%d injection sky points x %d spindowns (%.1f s)" %
                                               (len(inj_sky), nspin, t_cpu),
             "per_candidate": per}
-    print(json.dumps(line))
+    emit(line)
 
 
 def run_followup(args, L):
@@ -309,7 +309,7 @@ def run_followup(args, L):
                              "sample": "reference simplex (oracle restatement of followup.c amoeba, pinned to it) "
                                        "on %d candidates, %d evaluations, %.1f s" % (ncpu, cpu_nev, t_cpu)}}
     fu.close()
-    print(json.dumps(line))
+    emit(line)
 
 
 def run_segments(args, L):
@@ -385,10 +385,25 @@ def run_segments(args, L):
             "autotune": {"seconds": t_tune, "schedules": [list(x) for x in sched]},
             "candidates_identical_fixed_vs_tuned": bool(same)}
     seg.close()
-    print(json.dumps(line))
+    emit(line)
+
+
+_JSON_FD = 1
+
+
+def emit(line: dict) -> None:
+    """The one JSON result line, on the original standard output."""
+    os.write(_JSON_FD, (json.dumps(line) + "\n").encode())
 
 
 def main():
+    # the C host library reports its set-up on standard output, as the
+    # reference program does; send that to standard error so that standard
+    # output carries the JSON line only
+    global _JSON_FD
+    sys.stdout.flush()
+    _JSON_FD = os.dup(1)
+    os.dup2(2, 1)
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -463,7 +478,7 @@ def main():
                                  "sample": "%d sky points x %d spindowns per step (CPU oracle, OpenMP)" %
                                            (args.cpu_sky, nspin)},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        emit(line)
         return
 
     # N > 1: one replica of the whole workload per GPU (sky points are
@@ -603,7 +618,7 @@ def main():
                                 "index_mismatches": sum(1 for k in ref if k not in got and not edge(ref[k])) +
                                 sum(1 for k in got if k not in ref and not edge(got[k]))}
     if rank == 0:
-        print(json.dumps(out))
+        emit(out)
     ctx.close()
     replicas.shutdown()
 
