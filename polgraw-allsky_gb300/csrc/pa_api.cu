@@ -614,6 +614,9 @@ int enqueue_sky(pa_ctx* c, const SkyHost& h, const pa_opts* o, int task, void* F
     e = c->eng->spindowns(a, slot, Fss, 1, o->trl, o->white_flag, o->s0_flag, c->stream, Fdbg);
     if (e != cudaSuccess) return cuda_fail(c, e, "spindown launch");
   } else {
+    // full launches and one remainder: splitting into equal launches (200 as
+    // 4 x 50 instead of 3 x 64 + 8) was measured 1.5% slower, as each
+    // launch's last partial wave of CTAs costs a whole wave
     for (int ss = h.smin; ss <= h.smax; ss += c->b.sbatch) {
       const int nb = std::min(c->b.sbatch, h.smax - ss + 1);
       e = c->eng->spindowns(a, slot, ss, nb, o->trl, o->white_flag, o->s0_flag, c->stream, nullptr);
