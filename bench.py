@@ -242,8 +242,10 @@ def run_followup(args, L):
     pts, ws, which = workloads.candidates_around(host, inj, ncand)
     scale = np.median(ws, axis=0)
     res = {}
-    for name, prec in (("mixed", L.PA_PREC_MIXED), ("fp64", L.PA_PREC_FP64)):
-        fu = L.Followup(s, dets, nifo, precision=prec)
+    for name, prec, ph in (("mixed", L.PA_PREC_MIXED, L.PA_PHASE_F64),
+                           ("mixed_ffphase", L.PA_PREC_MIXED, L.PA_PHASE_FF),
+                           ("fp64", L.PA_PREC_FP64, L.PA_PHASE_F64)):
+        fu = L.Followup(s, dets, nifo, precision=prec, phase_mode=ph)
         for _ in range(max(1, args.warmup)):
             fu.fstatnet(pts)
         ms = 0.0
@@ -262,11 +264,13 @@ def run_followup(args, L):
                      "F": F, "grad": g}
         fu.close()
     # mixed-form gradient against the FP64 form, in peak-width units
-    gm, g64 = res["mixed"].pop("grad"), res["fp64"].pop("grad")
-    Fm, F64 = res["mixed"].pop("F"), res["fp64"].pop("F")
+    gm, g64, gff = res["mixed"].pop("grad"), res["fp64"].pop("grad"), res["mixed_ffphase"].pop("grad")
+    Fm, F64, Fff = res["mixed"].pop("F"), res["fp64"].pop("F"), res["mixed_ffphase"].pop("F")
     gscale = np.abs(scale * g64).max(axis=1)
     grad_err = float((np.abs(scale * (gm - g64)).max(axis=1) / gscale).max())
     F_err = float((np.abs(Fm - F64) / F64).max())
+    res["mixed_ffphase"]["F_rel_err_max_vs_fp64"] = float((np.abs(Fff - F64) / F64).max())
+    res["mixed_ffphase"]["grad_rel_err_max_vs_fp64"] = float((np.abs(scale * (gff - g64)).max(axis=1) / gscale).max())
     fu = L.Followup(s, dets, nifo, precision=L.PA_PREC_MIXED)
     launches0 = fu.launches()
     t0 = time.perf_counter()

@@ -72,7 +72,9 @@ struct FuCand {
   unsigned long long ffx, sfx;  // f/2pi, s/2pi in fixed-point turns
   double fo_t, st2;     // (f + oms)/2pi, 2s/2pi
   double nS[3];         // source unit vector
-  float nSf[3];         // FP32 copy (derivative factors)
+  float nSf[3];         // FP32 copy (derivative factors); hi parts of nS
+  float nSl[3];         // lo parts of nS (two-float phase)
+  float foh, fol, s2h, s2l;  // (f + oms)/2pi and 2s/2pi as two floats
   R nD[3], nA[3];       // d nS / d delta, d nS / d alpha
   R om0, s2;            // f + oms, 2 s (d phase / d shft = om0 + s2 i)
   // adjoint seeds: conj(X) parts and the factors of dF/dX, dF/dA
@@ -121,7 +123,14 @@ __global__ void k_fu_prep(const double* __restrict__ pts, int n, const unsigned 
   c.nS[0] = ca * cd;
   c.nS[1] = sa * cd;
   c.nS[2] = sd;
-  for (int j = 0; j < 3; j++) c.nSf[j] = (float)c.nS[j];
+  for (int j = 0; j < 3; j++) {
+    c.nSf[j] = (float)c.nS[j];
+    c.nSl[j] = (float)(c.nS[j] - (double)c.nSf[j]);
+  }
+  c.foh = (float)c.fo_t;
+  c.fol = (float)(c.fo_t - (double)c.foh);
+  c.s2h = (float)c.st2;
+  c.s2l = (float)(c.st2 - (double)c.s2h);
   c.nD[0] = (R)(-ca * sd);
   c.nD[1] = (R)(-sa * sd);
   c.nD[2] = (R)cd;
@@ -179,7 +188,8 @@ __global__ void k_fu_select(FuCand<R>* __restrict__ cand, int n, const unsigned 
 template <typename R>
 struct Sample {
   R x, cm, sm;
-  float r0f, r1f, r2f;   // FP32 copy of the position (derivative factors)
+  float r0f, r1f, r2f;   // FP32 copy of the position (derivative factors); hi parts
+  float r0l, r1l, r2l;   // lo parts (two-float phase)
   double r0, r1, r2;
   double di;             // the sample index as FP64
 };
@@ -212,6 +222,49 @@ __device__ __forceinline__ void fu_phase(const FuCand<R>& c, double oms, int i, 
   }
 }
 
+// Two-float (compensated) form of the mixed phase: shft = nS.R, the factor
+// (f + oms + 2 s i)/2pi and their product with float pairs (about 44
+// significant bits; error-free products by fma, sums by TwoSum), the product
+// reduced mod 1 exactly (Sterbenz) and added, as fixed point, to the exact
+// integer part [f i + s i^2]/2pi.  No FP64 operation per (point, sample).
+struct F2 {
+  float h, l;
+};
+__device__ __forceinline__ F2 f2_mul(float ah, float al, float bh, float bl) {
+  const float p = __fmul_rn(ah, bh);
+  float e = __fmaf_rn(ah, bh, -p);
+  e = __fmaf_rn(ah, bl, e);
+  e = __fmaf_rn(al, bh, e);
+  return F2{p, e};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  const float r = __fadd_rn(__fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb)), __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, r);
+  return F2{h, __fsub_rn(r, __fsub_rn(h, s))};
+}
+template <typename R>
+__device__ __forceinline__ void fu_phase_ff(const FuCand<R>& c, int i, const Sample<R>& v, R* sn, R* cs) {
+  // shft = sum_k nS_k R_k
+  F2 sh = f2_mul(c.nSf[0], c.nSl[0], v.r0f, v.r0l);
+  sh = f2_add(sh, f2_mul(c.nSf[1], c.nSl[1], v.r1f, v.r1l));
+  sh = f2_add(sh, f2_mul(c.nSf[2], c.nSl[2], v.r2f, v.r2l));
+  // w = (f + oms)/2pi + (2s/2pi) i  (i < 2^24 is exact in FP32)
+  const float fi = (float)i;
+  const F2 w = f2_add(F2{c.foh, c.fol}, f2_mul(c.s2h, c.s2l, fi, 0.f));
+  const F2 t = f2_mul(w.h, w.l, sh.h, sh.l);
+  // t mod 1: h - rint(h) is exact
+  const float fr = __fadd_rn(__fsub_rn(t.h, rintf(t.h)), t.l);
+  const unsigned long long ui = (unsigned long long)i;
+  const unsigned long long tt =
+      c.ffx * ui + c.sfx * (ui * ui) + ((unsigned long long)(long long)__float2ll_rn(fr * 4294967296.f) << 32);
+  float s_, c_;
+  sincospif((float)(int)(tt >> 32) * 4.656612873077393e-10f, &s_, &c_);
+  *sn = (R)s_;
+  *cs = (R)c_;
+}
+
 template <typename R>
 __device__ __forceinline__ R warp_sum(R v) {
 #pragma unroll
@@ -227,7 +280,7 @@ __device__ __forceinline__ R warp_sum(R v) {
 //                   + da/dtheta (x ka Re(conj(Xa)E) + 2 qa a) + (b terms) ]
 //   (x 1/sig2), with E = e^{-i phi}, ka = 2 seed/A, qa = -seed |Xa|^2/A^2.
 // ---------------------------------------------------------------------
-template <typename R, bool ADJ>
+template <typename R, bool ADJ, bool FF = false>
 __global__ void __launch_bounds__(kThreads) k_fu_sums(const R* __restrict__ xd, const double* __restrict__ pos,
                                                       const R* __restrict__ cmf, const R* __restrict__ smf,
                                                       const FuCand<R>* __restrict__ cand, const R* __restrict__ coef,
@@ -253,6 +306,9 @@ __global__ void __launch_bounds__(kThreads) k_fu_sums(const R* __restrict__ xd, 
     v.r0f = (float)v.r0;
     v.r1f = (float)v.r1;
     v.r2f = (float)v.r2;
+    v.r0l = (float)(v.r0 - (double)v.r0f);
+    v.r1l = (float)(v.r1 - (double)v.r1f);
+    v.r2l = (float)(v.r2 - (double)v.r2f);
     v.di = (double)i;
     sh[j] = v;
   }
@@ -280,9 +336,14 @@ __global__ void __launch_bounds__(kThreads) k_fu_sums(const R* __restrict__ xd, 
       const R c2 = cc * cc, cs = cc * ss;
       const R a = (R)2 * Q[2] * c2 + Q[3] * cs + Q[4] * cc + Q[5] * ss + Q[6];
       const R b = (R)2 * Q[7] * c2 + Q[8] * cs + Q[9] * cc + Q[10] * ss + Q[11];
-      const double shft = c.nS[0] * v.r0 + c.nS[1] * v.r1 + c.nS[2] * v.r2;
       R sn, co;
-      fu_phase<R>(c, oms, i, v.di, shft, &sn, &co);
+      double shft = 0.;
+      if (FF) {
+        fu_phase_ff<R>(c, i, v, &sn, &co);
+      } else {
+        shft = c.nS[0] * v.r0 + c.nS[1] * v.r1 + c.nS[2] * v.r2;
+        fu_phase<R>(c, oms, i, v.di, shft, &sn, &co);
+      }
       if (!ADJ) {
         const R xa = v.x * a, xb = v.x * b;
         acc[0] += xa * co;
@@ -303,7 +364,8 @@ __global__ void __launch_bounds__(kThreads) k_fu_sums(const R* __restrict__ xd, 
         // position in the mixed form: no per-sample conversions)
         const R r0 = sizeof(R) == 4 ? (R)v.r0f : (R)v.r0, r1 = sizeof(R) == 4 ? (R)v.r1f : (R)v.r1,
                 r2 = sizeof(R) == 4 ? (R)v.r2f : (R)v.r2;
-        const R sh_ = sizeof(R) == 4 ? (R)(c.nSf[0] * v.r0f + c.nSf[1] * v.r1f + c.nSf[2] * v.r2f) : (R)shft;
+        const R sh_ = (sizeof(R) == 4 || FF) ? (R)(c.nSf[0] * v.r0f + c.nSf[1] * v.r1f + c.nSf[2] * v.r2f)
+                                             : (R)shft;
         const R sh_de = c.nD[0] * r0 + c.nD[1] * r1 + c.nD[2] * r2;
         const R sh_al = c.nA[0] * r0 + c.nA[1] * r1;
         const R om = c.om0 + c.s2 * fi;
@@ -537,6 +599,7 @@ __global__ void k_asc_export(const AscentState* __restrict__ st, int n, double* 
 struct pa_followup {
   int dev = 0;
   bool fp64 = false;
+  bool ffphase = false;  // mixed form with the two-float phase
   int N = 0, nifo = 0, nch = 0;
   double oms = 0.;
   FuDets dets;
@@ -635,6 +698,20 @@ static size_t fu_smem() {
   return sizeof(Sample<R>) * kChunk;
 }
 
+// One launch of the sums kernel in the context's phase form.
+template <typename R, bool ADJ>
+static void fu_sums(pa_followup* f, int n, dim3 grid) {
+  FuCand<R>* cand = (FuCand<R>*)f->cand;
+  if (sizeof(R) == 4 && f->ffphase)
+    k_fu_sums<R, ADJ, true><<<grid, kThreads, fu_smem<R>(), f->stream>>>(
+        (const R*)f->xd, f->pos, (const R*)f->cm, (const R*)f->sm, cand, (const R*)f->coef, f->dets, n, f->N,
+        f->nifo, f->nch, f->oms, f->part);
+  else
+    k_fu_sums<R, ADJ, false><<<grid, kThreads, fu_smem<R>(), f->stream>>>(
+        (const R*)f->xd, f->pos, (const R*)f->cm, (const R*)f->sm, cand, (const R*)f->coef, f->dets, n, f->N,
+        f->nifo, f->nch, f->oms, f->part);
+}
+
 // Forward (and optionally adjoint) evaluation of n points already in
 // f->pts; mask (device, may be null) selects the active points.
 template <typename R>
@@ -645,16 +722,12 @@ static int fu_eval_t(pa_followup* f, int n, const unsigned char* mask, bool want
   k_fu_prep<R><<<(n + 127) / 128, 128, 0, f->stream>>>(f->pts, n, mask, cand, (R*)f->coef, f->dets, f->nifo,
                                                           f->oms);
   dim3 grid(P, (n + kCandPerCta - 1) / kCandPerCta);
-  k_fu_sums<R, false><<<grid, kThreads, fu_smem<R>(), f->stream>>>(
-      (const R*)f->xd, f->pos, (const R*)f->cm, (const R*)f->sm, cand, (const R*)f->coef, f->dets, n, f->N,
-      f->nifo, f->nch, f->oms, f->part);
+  fu_sums<R, false>(f, n, grid);
   k_fu_final<R><<<(n + 7) / 8, 256, 0, f->stream>>>(f->part, f->pts, cand, n, P, f->res, f->F,
                                                      want_out ? f->out : nullptr, seed_dev);
   f->launches += 3;
   if (adjoint) {
-    k_fu_sums<R, true><<<grid, kThreads, fu_smem<R>(), f->stream>>>(
-        (const R*)f->xd, f->pos, (const R*)f->cm, (const R*)f->sm, cand, (const R*)f->coef, f->dets, n, f->N,
-        f->nifo, f->nch, f->oms, f->part);
+    fu_sums<R, true>(f, n, grid);
     k_fu_final_adj<R><<<(n + 7) / 8, 256, 0, f->stream>>>(f->part, cand, n, P, f->grad);
     f->launches += 2;
   }
@@ -669,9 +742,7 @@ static int fu_adjoint_t(pa_followup* f, int n, const unsigned char* need) {
   FuCand<R>* cand = (FuCand<R>*)f->cand;
   k_fu_select<R><<<(n + 255) / 256, 256, 0, f->stream>>>(cand, n, need);
   dim3 grid(P, (n + kCandPerCta - 1) / kCandPerCta);
-  k_fu_sums<R, true><<<grid, kThreads, fu_smem<R>(), f->stream>>>(
-      (const R*)f->xd, f->pos, (const R*)f->cm, (const R*)f->sm, cand, (const R*)f->coef, f->dets, n, f->N,
-      f->nifo, f->nch, f->oms, f->part);
+  fu_sums<R, true>(f, n, grid);
   k_fu_final_adj<R><<<(n + 7) / 8, 256, 0, f->stream>>>(f->part, cand, n, P, f->grad);
   f->launches += 3;
   FCK(cudaGetLastError(), "followup adjoint launch");
@@ -722,6 +793,7 @@ pa_followup* pa_followup_create(const pa_settings* sett, const pa_detector* det,
   f = new pa_followup();
   f->dev = c.device;
   f->fp64 = c.precision == PA_PREC_FP64;
+  f->ffphase = !f->fp64 && c.phase_mode == PA_PHASE_FF;
   f->N = sett->N;
   f->nifo = nifo;
   f->nch = (sett->N + kChunk - 1) / kChunk;
@@ -778,8 +850,10 @@ pa_followup* pa_followup_create(const pa_settings* sett, const pa_detector* det,
     cudaFuncSetAttribute(k_fu_sums<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_fu_sums<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   } else {
-    cudaFuncSetAttribute(k_fu_sums<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_fu_sums<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fu_sums<float, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fu_sums<float, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fu_sums<float, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_fu_sums<float, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return bail("set-up", e);
   if (status) *status = PA_OK;

@@ -468,9 +468,12 @@ class Followup:
     Fstatnet), its adjoint gradient, gradient ascent and the batched
     reference simplex.  Points are rows (f, s, delta, alpha)."""
 
-    def __init__(self, settings: Settings, dets, nifo: int, precision: int = PA_PREC_MIXED, device: int = 0):
+    def __init__(self, settings: Settings, dets, nifo: int, precision: int = PA_PREC_MIXED, device: int = 0,
+                 phase_mode: int = PA_PHASE_F64):
+        """phase_mode: PA_PHASE_F64 (FP64 phase, the default) or PA_PHASE_FF
+        (compensated two-float phase) in the mixed precision."""
         self.lib = load()
-        cfg = Config(precision, PA_PHASE_F64, 0, device)
+        cfg = Config(precision, phase_mode, 0, device)
         st = C.c_int(0)
         self.fu = self.lib.pa_followup_create(C.byref(settings), dets, nifo, C.byref(cfg), C.byref(st))
         if not self.fu:
