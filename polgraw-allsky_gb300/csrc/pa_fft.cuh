@@ -335,7 +335,9 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s = reinterpret_cast<T*>(smem_raw);
   T* tws = s + G::L2 * P;
-  const int batch = blockIdx.y;
+  // batches in reverse launch order: pass A wrote the last batch items
+  // last, so their intermediate is the likeliest to be still in L2
+  const int batch = gridDim.y - 1 - blockIdx.y;
   const int k10 = blockIdx.x << G::LOGRR;
   for (int m = threadIdx.x; m < G::L2; m += NT) tws[m] = tw2[m];
   const T* yb = ybuf + ((size_t)batch << (LOGL + 1));
