@@ -406,6 +406,85 @@ def run_segments(args, L):
     emit(line)
 
 
+def run_coinc(args, L):
+    """Coincidence workload (consumer of the trigger files): 24 frames x
+    2^20 trigger records (25.2 M records, 1.0 GB), N=86164 band 666, 64
+    frequency lines x 256 sky positions, 1000 signals, mincoin 4.  A step is
+    one pa_coinc_run over the resident records (cells, per-frame duplicate
+    removal, coincidences, records); `e2e` adds the upload of every frame
+    from pinned host memory and the read-back of the coincidence records."""
+    import torch
+    w = workloads.coincidences(args.coinc_frames, args.coinc_records)
+    cfg = L.coinc_cfg(N=w["N"], oms=w["oms"], vedva_m=L.vedva(w["fisher"]), refr=w["refr"], mincoin=w["mincoin"])
+    frames = w["frames"]
+    # pinned host copies of the trigger records
+    pinned = {}
+    for f in frames:
+        t = torch.empty((len(w["recs"][f]), 5), dtype=torch.float64, pin_memory=True)
+        t.numpy()[:] = w["recs"][f]
+        pinned[f] = t.numpy()
+    nrec = sum(len(v) for v in w["recs"].values())
+    cc = L.Coinc(cfg)
+    for f in frames:
+        cc.add_frame(f, pinned[f])
+    for _ in range(args.warmup):
+        cc.run()
+    l0 = cc.launches()
+    clocks = ClockSampler(0)
+    ms = 0.0
+    for _ in range(args.steps):
+        l2_flush()
+        res = cc.run()
+        ms += cc.last_call_ms()
+    clk = clocks.stop()
+    launches = (cc.launches() - l0) // max(1, args.steps)
+    value = nrec * args.steps / (ms / 1e3)
+    # end to end: upload, run, results back
+    t_e2e = 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cc.reset()
+        for f in frames:
+            cc.add_frame(f, pinned[f])
+        res = cc.run()
+        t_e2e += time.perf_counter() - t0
+    s = res.summary
+    d2h = int(s.ncoin) * 48 + int(s.nmembers) * 8 + 12 * len(frames)
+    # the CPU oracle on a bounded sample (the first records of every frame),
+    # and the device on the same sample
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    sub = {f: np.ascontiguousarray(w["recs"][f][:args.coinc_cpu_records]) for f in frames}
+    t0 = time.perf_counter()
+    ora = pyoracle.coinc(cfg, frames, [sub[f] for f in frames])
+    t_cpu = time.perf_counter() - t0
+    nsub = sum(len(v) for v in sub.values())
+    cs = L.Coinc(cfg)
+    for f in frames:
+        cs.add_frame(f, sub[f])
+    dev = cs.run()
+    cs.close()
+    same = dev.coi_bytes() == ora.coi_bytes() and dev.frameinfo.tolist() == ora.frameinfo.tolist()
+    line = {"metric": "trigger records/s through the coincidence step (cells, duplicate removal, coincidences)",
+            "value": value, "unit": "records/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 cells, u64 keys", "data": "synthetic",
+            "config": {"workload": "%d frames x %d trigger records, N=86164, 64 lines x 256 sky, 1000 signals, "
+                                   "mincoin 4" % (len(frames), args.coinc_records),
+                       "records": nrec, "inband": int(s.inband), "unique": int(s.unique), "coincidences": int(s.ncoin),
+                       "maxcoin": int(s.maxcoin),
+                       "l2": "flushed (256 MB write) before each timed step; records 1.0 GB > L2"},
+            "clocks": clk, "gpu_launches": int(launches),
+            "e2e": {"value": nrec * args.steps / t_e2e, "unit": "records/s", "h2d_bytes_per_step": 40 * nrec,
+                    "d2h_bytes_per_step": d2h},
+            "cpu_baseline": {"value": nsub / t_cpu, "unit": "records/s", "cores": 1, "kind": "port",
+                             "sample": "first %d records of each of the %d frames (CPU oracle, one thread, %.1f s)" %
+                                       (args.coinc_cpu_records, len(frames), t_cpu)},
+            "matches_oracle_on_sample": bool(same)}
+    cc.close()
+    emit(line)
+
+
 _JSON_FD = 1
 
 
@@ -435,7 +514,12 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--schedule", default="", help="fixed spindown schedule 'sbatch,split' (skips the autotuner)")
     ap.add_argument("--segments", type=int, default=24, help="segments workload: number of segments")
-    ap.add_argument("--workload", default="network", choices=["network", "stress", "followup", "segments"],
+    ap.add_argument("--coinc-frames", type=int, default=24, help="coincidences workload: frames")
+    ap.add_argument("--coinc-records", type=int, default=1 << 20, help="coincidences workload: records per frame")
+    ap.add_argument("--coinc-cpu-records", type=int, default=100000,
+                    help="coincidences workload: records per frame in the CPU-oracle sample")
+    ap.add_argument("--workload", default="network",
+                    choices=["network", "stress", "followup", "segments", "coincidences"],
                     help="stress: the N=258492 precision-stress workload, every precision form; "
                          "followup: demodulated F-statistic, adjoint, ascent and simplex on 4096 candidates")
     ap.add_argument("--candidates", type=int, default=4096, help="followup workload: candidates")
@@ -460,6 +544,10 @@ def main():
     if args.workload == "segments":
         if rank == 0:
             run_segments(args, L)
+        return
+    if args.workload == "coincidences":
+        if rank == 0:
+            run_coinc(args, L)
         return
     tmp = tempfile.mkdtemp(prefix="pa_bench_")
     argv = make_workload(tmp, args.spindowns)

@@ -34,6 +34,8 @@ extern "C" {
 #define PA_NAV 4096          /* settings.h:12: nmin/nmax edge width (x B) */
 #define PA_NAVFSTAT 4096     /* auxi.h:8: F-statistic normalisation block */
 #define PA_MAXL 2048         /* struct.h:13: maximum number of veto lines */
+/* settings.h:14,20: mean obliquity of the ecliptic, the epsm of ast2lin() */
+#define PA_C_EPSMA (84381.448 / 3600. / (180 / M_PI))
 
 typedef enum pa_status {
   PA_OK = 0,
@@ -357,6 +359,86 @@ int pa_followup_simplex(pa_followup *fu, double *sgnlo, int n, const double *pc2
  * the number of kernel launches so far. */
 double pa_followup_last_call_ms(const pa_followup *fu);
 long long pa_followup_kernel_launches(const pa_followup *fu);
+
+/* ------------------------------------------------------------------------
+ * Coincidences among the trigger files of several time frames (segments):
+ * the consumer of the search's trigger files, read_trigger_files() of
+ * coincidences/src/coincidences.c:117-600, with the per-trigger cell
+ * assignment, the per-frame duplicate removal and the coincidence count on
+ * the device.  The trigger files themselves are read unchanged (5 doubles
+ * f, s, delta, alpha, SNR per record: coincidences.c:229).
+ * ------------------------------------------------------------------------ */
+
+typedef struct pa_coinc pa_coinc;
+
+typedef struct pa_coinc_cfg {
+  int N;                   /* samples of a segment, search_settings() (settings.c:32) */
+  double oms;              /* 2 pi fpo dt (settings.c:28) */
+  double vedva[4][4];      /* eigenvectors x sqrt(eigenvalues) of the grid's
+                              Fisher matrix (init.c:1195-1210); see pa_coinc_vedva */
+  int shift[4];            /* cell shifts in f, s, delta, alpha (digits of -shift) */
+  int scale[4];            /* cell scaling (digits of -scale; a 0 digit means 1) */
+  int refr;                /* reference frame number (-refr) */
+  double narrowdown;       /* half-width of the kept band around pi/2, radians
+                              (-narrowdown times pi, init.c:1111) */
+  double snrcutoff;        /* keep SNR > snrcutoff (-snrcutoff) */
+  int mincoin;             /* minimal coincidence multiplicity (-mincoin, >= 1) */
+  int device;              /* CUDA device ordinal */
+} pa_coinc_cfg;
+
+/* One coincidence as coincidences.c:488-541 writes it: multiplicity w, the
+ * FP64 means of f, s, delta, alpha over the members and sqrt of the sum of
+ * squared SNRs (the file stores them as float), and the offset of its w
+ * members in the member arrays (frame numbers and record positions, in the
+ * reference's order). */
+typedef struct pa_coinc_rec {
+  int w;
+  int first;               /* index of the first member */
+  double mean[5];
+} pa_coinc_rec;
+
+/* Sizes and per-frame counts after pa_coinc_run(). */
+typedef struct pa_coinc_summary {
+  int nframes;
+  long long raw;           /* records read */
+  long long inband;        /* records passing the band and SNR cuts */
+  long long unique;        /* records left after the per-frame duplicate removal */
+  int ncoin;               /* coincidence records to write (coincidences.c:488) */
+  long long nmembers;      /* sum of their multiplicities */
+  int maxcoin;             /* largest multiplicity (0: none) */
+  int maxcoin_index;       /* record with maxcoin and the largest mean SNR */
+} pa_coinc_summary;
+
+/* Host: vedva[i][j] = eigvec[i][j] sqrt(eigval[j]) of the symmetric 4x4
+ * matrix fisher[16] (row-major; the second matrix of grid.bin,
+ * init.c:1167-1172), by cyclic Jacobi rotations (eigenvalues in the order
+ * the rotations leave them, no sorting). */
+int pa_coinc_vedva(const double *fisher, double *vedva);
+
+pa_coinc *pa_coinc_create(const pa_coinc_cfg *cfg, int *status);
+void pa_coinc_destroy(pa_coinc *cc);
+const char *pa_coinc_last_error(const pa_coinc *cc);
+/* Starts a new set of frames (keeps the device buffers). */
+int pa_coinc_reset(pa_coinc *cc);
+/* Appends one trigger file's records (host memory, n x 5 doubles) as frame
+ * `frame` (the number parsed from the file name, coincidences.c:206-215);
+ * frames are taken in the order they are added (the reference's directory
+ * order).  At most 255 frames (Candidate_triggers.frameinfo[256]). */
+int pa_coinc_add_frame(pa_coinc *cc, int frame, const double *records, long long n);
+/* Cells, duplicate removal, coincidences.  Fills *sum. */
+int pa_coinc_run(pa_coinc *cc, pa_coinc_summary *sum);
+/* Results of the last run, each array optional (NULL): per-frame
+ * frameinfo[nframes][3] = {frame, in-band, unique} (coincidences.c:305-421);
+ * recs[ncoin]; member frame numbers fra[nmembers] and record positions
+ * ops[nmembers] (position in the frame's trigger file). */
+int pa_coinc_get(const pa_coinc *cc, int *frameinfo, pa_coinc_rec *recs, int *fra, int *ops);
+/* The pre-binning itself: for the in-band records of the last run in read
+ * order (frame by frame), cells[inband][4] (fi, si, di, ai of
+ * coincidences.c:256-261) and keep[inband] = 1 for the record each
+ * frame's duplicate removal keeps. */
+int pa_coinc_cells(const pa_coinc *cc, int *cells, unsigned char *keep);
+double pa_coinc_last_call_ms(const pa_coinc *cc);
+long long pa_coinc_kernel_launches(const pa_coinc *cc);
 
 #ifdef __cplusplus
 }

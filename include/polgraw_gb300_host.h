@@ -70,6 +70,13 @@ void pa_host_core_opts(const pa_host *h, pa_opts *out);
 void pa_host_config(const pa_host *h, pa_config *out);
 const char *pa_host_detector_name(const pa_host *h, int i);
 
+/* The coincidence program coincidences-gb300 (coincidences/src/
+ * coincidences.c main and read_trigger_files, init.c handle_opts_coinc and
+ * manage_grid_matrix) over the device coincidence step pa_coinc_*: same
+ * options, directory scan, .coi output and stderr summary.  Returns the
+ * process exit code. */
+int pa_coinc_main(int argc, char **argv);
+
 #ifdef __cplusplus
 }
 #endif

@@ -56,13 +56,14 @@ def _newer(target: str, sources: list[str]) -> bool:
 
 def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    srcs = [os.path.join(HERE, f) for f in ("oracle.c", "fft.c")]
-    deps = srcs + [os.path.join(HERE, f) for f in ("oracle.h", "fft.h")] + [
+    srcs = [os.path.join(HERE, f) for f in ("oracle.c", "fft.c", "oracle_coinc.c", "shim/gsl_shim.c")]
+    deps = srcs + [os.path.join(HERE, f) for f in ("oracle.h", "fft.h", "shim/gsl/pa_gsl_shim.h")] + [
         os.path.join(HERE, "..", "include", "polgraw_gb300.h")]
     if force or _newer(ORACLE_LIB, deps):
         tmp = ORACLE_LIB + ".tmp%d" % os.getpid()
         _run([_CC, "-std=gnu11", "-O2", "-fPIC", "-shared", "-fopenmp",
-              "-ffp-contract=off", "-Wall", "-Wno-unused", "-o", tmp] + srcs + ["-lm"])
+              "-ffp-contract=off", "-Wall", "-Wno-unused", "-I" + os.path.join(HERE, "shim"),
+              "-o", tmp] + srcs + ["-lm"])
         os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
 
@@ -129,6 +130,37 @@ def _build_ref_followup() -> str:
     return REF_FOLLOWUP
 
 
+REF_COINC = os.path.join(REF_OUT, "coincidences-ref")
+
+
+def _build_ref_coinc() -> str:
+    """The reference coincidence program (coincidences/src/coincidences.c
+    with the network search's settings.c, auxi.c and init.c, as its Makefile
+    links them), unmodified, against the FFTW/GSL shims (the eigensystem of
+    manage_grid_matrix comes from oracle/shim/gsl_shim.c)."""
+    co = os.path.join(REFERENCE_ROOT, "coincidences", "src")
+    sd = os.path.join(NETWORK, "src-cpu")
+    srcs = [os.path.join(co, "coincidences.c")] + [os.path.join(sd, n) for n in ("settings.c", "auxi.c", "init.c")]
+    mine = [os.path.join(HERE, "shim", "fftw_shim.c"), os.path.join(HERE, "shim", "gsl_shim.c"),
+            os.path.join(HERE, "fft.c")]
+    if not _newer(REF_COINC, srcs + mine):
+        return REF_COINC
+    os.makedirs(REF_OUT, exist_ok=True)
+    objdir = os.path.join(REF_OUT, "obj_coinc")
+    os.makedirs(objdir, exist_ok=True)
+    cflags = ["-std=gnu11", "-fcommon", "-O2", "-ffp-contract=off", "-fno-builtin", "-DGNUSINCOS",
+              "-DPREFIX=./coinc-results", "-DDTAPREFIX=./candidates", "-DCODEVER=reference",
+              "-I" + os.path.join(HERE, "shim"), "-I" + sd, "-w"]
+    objs = []
+    for k, src in enumerate(srcs + mine):
+        o = os.path.join(objdir, "%d_%s" % (k, os.path.basename(src).replace(".c", ".o")))
+        _run([_CC] + cflags + ["-c", src, "-o", o])
+        objs.append(o)
+    _run([_CC, "-o", REF_COINC] + objs + ["-lm"])
+    shutil.rmtree(objdir, ignore_errors=True)
+    return REF_COINC
+
+
 def build_reference() -> dict:
     """Compile the reference search (serial parity build and OpenMP timing
     build).  Returns {} when the reference checkout is absent."""
@@ -146,6 +178,7 @@ def build_reference() -> dict:
     out["omp"] = _build_ref_variant(
         "src-openmp", REF_OMP, ["-O3", "-ffast-math", "-fopenmp", "-fno-builtin", "-DTIMERS=3"])
     out["followup"] = _build_ref_followup()
+    out["coinc"] = _build_ref_coinc()
     return out
 
 

@@ -78,6 +78,20 @@ double ora_fstatnet_grad(ora_ctx *c, const double sgnlo[4], double grad[4]);
 int ora_amoeba(ora_ctx *c, double point[4], const double pc2[4], double tol, int max_evals,
                double out[11]);
 
+/* Coincidences (coincidences/src/coincidences.c:117-600), oracle_coinc.c.
+ * ora_coinc_vedva: manage_grid_matrix()'s transformation matrix
+ *   (init.c:1185-1210) through the GSL shim's eigensystem.
+ * ora_coinc_run: all frames in the given order (the reference's directory
+ *   order); results read back like pa_coinc_get / pa_coinc_cells. */
+typedef struct ora_coinc ora_coinc;
+int ora_coinc_vedva(const double *fisher, double *vedva);
+ora_coinc *ora_coinc_run(const pa_coinc_cfg *cfg, int nframes, const int *frames,
+                         const double *const *recs, const long long *nrec,
+                         pa_coinc_summary *sum);
+int ora_coinc_get(const ora_coinc *o, int *frameinfo, pa_coinc_rec *recs, int *fra, int *ops);
+int ora_coinc_cells(const ora_coinc *o, int *cells, unsigned char *keep);
+void ora_coinc_free(ora_coinc *o);
+
 #ifdef __cplusplus
 }
 #endif

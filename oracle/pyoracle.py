@@ -156,3 +156,61 @@ class FollowupOracle(Oracle):
         out = np.zeros(11)
         nev = self.lib.ora_amoeba(self.o, _dp(p), _dp(st), tol, max_evals, _dp(out))
         return p, out, nev
+
+
+def _coinc_bind(lib):
+    if getattr(lib, "_coinc_bound", False):
+        return lib
+    P = C.POINTER
+    lib.ora_coinc_vedva.argtypes = [P(C.c_double), P(C.c_double)]
+    lib.ora_coinc_run.restype = C.c_void_p
+    lib.ora_coinc_run.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(P(C.c_double)), P(C.c_longlong), C.c_void_p]
+    lib.ora_coinc_get.argtypes = [C.c_void_p, P(C.c_int), C.c_void_p, P(C.c_int), P(C.c_int)]
+    lib.ora_coinc_cells.argtypes = [C.c_void_p, P(C.c_int), P(C.c_ubyte)]
+    lib.ora_coinc_free.argtypes = [C.c_void_p]
+    lib.ora_coinc_free.restype = None
+    lib._coinc_bound = True
+    return lib
+
+
+def coinc_vedva(fisher) -> np.ndarray:
+    """manage_grid_matrix()'s vedva through the GSL shim's eigensystem."""
+    lib = _coinc_bind(load())
+    f = np.ascontiguousarray(np.asarray(fisher, dtype=np.float64).reshape(16))
+    out = np.zeros(16)
+    lib.ora_coinc_vedva(_dp(f), _dp(out))
+    return out.reshape(4, 4)
+
+
+def coinc(cfg, frames, recs) -> "object":
+    """The coincidence step on the CPU over frames in the given order;
+    returns the product's CoincResult type (cells included)."""
+    from importlib import import_module
+    L = import_module("polgraw_gb300.lib")
+    lib = _coinc_bind(load())
+    arrs = [np.ascontiguousarray(np.asarray(r, dtype=np.float64).reshape(-1, 5)) for r in recs]
+    nf = len(arrs)
+    fr = (C.c_int * max(1, nf))(*[int(x) for x in frames])
+    ptrs = (C.POINTER(C.c_double) * max(1, nf))(*[_dp(a) for a in arrs])
+    ns = (C.c_longlong * max(1, nf))(*[len(a) for a in arrs])
+    s = L.CoincSummary()
+    o = lib.ora_coinc_run(C.byref(cfg), nf, fr, ptrs, ns, C.byref(s))
+    if not o:
+        raise RuntimeError("ora_coinc_run: invalid arguments")
+    try:
+        IP = C.POINTER(C.c_int)
+        fi = np.zeros((max(1, s.nframes), 3), dtype=np.int32)
+        rr = (L.CoincRec * max(1, s.ncoin))()
+        fra = np.zeros(max(1, s.nmembers), dtype=np.int32)
+        ops = np.zeros(max(1, s.nmembers), dtype=np.int32)
+        lib.ora_coinc_get(o, fi.ctypes.data_as(IP), rr, fra.ctypes.data_as(IP), ops.ctypes.data_as(IP))
+        cl = np.zeros((max(1, s.inband), 4), dtype=np.int32)
+        kp = np.zeros(max(1, s.inband), dtype=np.uint8)
+        lib.ora_coinc_cells(o, cl.ctypes.data_as(IP), kp.ctypes.data_as(C.POINTER(C.c_ubyte)))
+    finally:
+        lib.ora_coinc_free(o)
+    w = np.array([rr[q].w for q in range(s.ncoin)], dtype=np.int32)
+    first = np.array([rr[q].first for q in range(s.ncoin)], dtype=np.int64)
+    mean = np.array([list(rr[q].mean) for q in range(s.ncoin)], dtype=np.float64).reshape(-1, 5)
+    return L.CoincResult(s, fi[:s.nframes], w, first, mean, fra[:s.nmembers], ops[:s.nmembers],
+                         cl[:s.inband], kp[:s.inband])

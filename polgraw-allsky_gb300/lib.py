@@ -35,6 +35,9 @@ EXPORTS = [
     "pa_segments_last_call_ms",
     "pa_followup_create", "pa_followup_destroy", "pa_followup_last_error", "pa_fstatnet", "pa_fstatnet_grad",
     "pa_followup_ascent", "pa_followup_simplex", "pa_followup_last_call_ms", "pa_followup_kernel_launches",
+    "pa_coinc_vedva", "pa_coinc_create", "pa_coinc_destroy", "pa_coinc_last_error", "pa_coinc_reset",
+    "pa_coinc_add_frame", "pa_coinc_run", "pa_coinc_get", "pa_coinc_cells", "pa_coinc_last_call_ms",
+    "pa_coinc_kernel_launches", "pa_coinc_main",
 ]
 
 
@@ -71,6 +74,21 @@ class Config(C.Structure):
 
 class Sky(C.Structure):
     _fields_ = [("pm", C.c_int), ("mm", C.c_int), ("nn", C.c_int)]
+
+
+class CoincCfg(C.Structure):
+    _fields_ = [("N", C.c_int), ("oms", C.c_double), ("vedva", C.c_double * 16), ("shift", C.c_int * 4),
+                ("scale", C.c_int * 4), ("refr", C.c_int), ("narrowdown", C.c_double), ("snrcutoff", C.c_double),
+                ("mincoin", C.c_int), ("device", C.c_int)]
+
+
+class CoincRec(C.Structure):
+    _fields_ = [("w", C.c_int), ("first", C.c_int), ("mean", C.c_double * 5)]
+
+
+class CoincSummary(C.Structure):
+    _fields_ = [("nframes", C.c_int), ("raw", C.c_longlong), ("inband", C.c_longlong), ("unique", C.c_longlong),
+                ("ncoin", C.c_int), ("nmembers", C.c_longlong), ("maxcoin", C.c_int), ("maxcoin_index", C.c_int)]
 
 
 _lib = None
@@ -145,6 +163,22 @@ def load(path: str | None = None) -> C.CDLL:
     lib.pa_followup_last_call_ms.argtypes = [C.c_void_p]
     lib.pa_followup_kernel_launches.restype = C.c_longlong
     lib.pa_followup_kernel_launches.argtypes = [C.c_void_p]
+    lib.pa_coinc_vedva.argtypes = [P(C.c_double), P(C.c_double)]
+    lib.pa_coinc_create.restype = C.c_void_p
+    lib.pa_coinc_create.argtypes = [P(CoincCfg), P(C.c_int)]
+    lib.pa_coinc_destroy.argtypes = [C.c_void_p]
+    lib.pa_coinc_destroy.restype = None
+    lib.pa_coinc_last_error.restype = C.c_char_p
+    lib.pa_coinc_last_error.argtypes = [C.c_void_p]
+    lib.pa_coinc_reset.argtypes = [C.c_void_p]
+    lib.pa_coinc_add_frame.argtypes = [C.c_void_p, C.c_int, P(C.c_double), C.c_longlong]
+    lib.pa_coinc_run.argtypes = [C.c_void_p, P(CoincSummary)]
+    lib.pa_coinc_get.argtypes = [C.c_void_p, P(C.c_int), P(CoincRec), P(C.c_int), P(C.c_int)]
+    lib.pa_coinc_cells.argtypes = [C.c_void_p, P(C.c_int), P(C.c_ubyte)]
+    lib.pa_coinc_last_call_ms.restype = C.c_double
+    lib.pa_coinc_last_call_ms.argtypes = [C.c_void_p]
+    lib.pa_coinc_kernel_launches.restype = C.c_longlong
+    lib.pa_coinc_kernel_launches.argtypes = [C.c_void_p]
     lib.pa_host_create.restype = C.c_void_p
     lib.pa_host_create.argtypes = [C.c_int, P(C.c_char_p), P(C.c_int)]
     lib.pa_host_setup.argtypes = [C.c_void_p]
@@ -585,3 +619,168 @@ def make_detectors(xdats, detssbs, sig2s, sphirs, cphirs, amods):
         for k in range(9):
             arr[i].amod[k] = amods[i][k]
     return arr, keep
+
+
+# ---------------------------------------------------------------------------
+# Coincidences among frames (pa_coinc_*, coincidences/src/coincidences.c)
+# ---------------------------------------------------------------------------
+
+def digits4(val: int, default: int) -> list[int]:
+    """The four per-direction digits of -shift / -scale (coincidences.c:157-178):
+    read from the right, a 0 digit keeps the default."""
+    d = [default] * 4
+    i = 3
+    while val > 0 and i >= 0:
+        if val % 10:
+            d[i] = val % 10
+        i -= 1
+        val //= 10
+    return d
+
+
+def read_fisher(grid_path: str) -> np.ndarray:
+    """The second 4x4 matrix of grid.bin (manage_grid_matrix, init.c:1155-1167)."""
+    raw = open(grid_path, "rb").read()
+    return np.frombuffer(raw[4 + 128:4 + 256], dtype="<f8").reshape(4, 4).copy()
+
+
+def vedva(fisher) -> np.ndarray:
+    """pa_coinc_vedva: eigenvectors x sqrt(eigenvalues) of the Fisher matrix."""
+    f = np.ascontiguousarray(np.asarray(fisher, dtype=np.float64).reshape(16))
+    out = np.zeros(16)
+    rc = load().pa_coinc_vedva(_dp(f), _dp(out))
+    if rc != PA_OK:
+        raise SearchError("pa_coinc_vedva failed (%d)" % rc)
+    return out.reshape(4, 4)
+
+
+def coinc_cfg(*, N: int, oms: float, vedva_m, shift: int = 0, scale: int = 1111, refr: int = 1,
+              narrowdown: float = 0.5, snrcutoff: float = 6.0, mincoin: int = 3, device: int = 0) -> CoincCfg:
+    """pa_coinc_cfg from the coincidence program's options (handle_opts_coinc,
+    init.c:972-1122): narrowdown in units of pi as on the command line."""
+    import math
+    c = CoincCfg()
+    c.N = N
+    c.oms = oms
+    for i, v in enumerate(np.asarray(vedva_m, dtype=np.float64).reshape(16)):
+        c.vedva[i] = float(v)
+    for i, v in enumerate(digits4(int(shift), 0)):
+        c.shift[i] = v
+    for i, v in enumerate(digits4(int(scale), 1)):
+        c.scale[i] = v
+    c.refr = refr
+    c.narrowdown = narrowdown * math.pi
+    c.snrcutoff = snrcutoff
+    c.mincoin = mincoin
+    c.device = device
+    return c
+
+
+class CoincResult:
+    """Output of a coincidence run: per-frame counts, the records in file
+    order (multiplicity w, FP64 means), and their members."""
+
+    def __init__(self, summary, frameinfo, w, first, mean, fra, ops, cells=None, keep=None):
+        self.summary = summary
+        self.frameinfo = frameinfo
+        self.w = w
+        self.first = first
+        self.mean = mean
+        self.fra = fra
+        self.ops = ops
+        self.cells = cells
+        self.keep = keep
+
+    def summary_line(self, trigname: str, shift: int, fpo: float) -> str:
+        """The line the coincidence program writes to stderr for the largest
+        coincidence with the largest mean SNR (coincidences.c:547-593), or ""
+        when no coincidence reaches mincoin."""
+        s = self.summary
+        if s.ncoin == 0 or s.maxcoin < 1:
+            return ""
+        q = s.maxcoin_index
+        m = self.mean[q]
+        line = "%s %04d %5f %5d %5d %15.8e %5.8e %5.8e %5.8e %5e " % (
+            trigname, shift, fpo, s.nframes & 0xFFFF, s.maxcoin, m[0], m[1], m[2], m[3], m[4])
+        for fi in self.frameinfo:
+            line += "%d %d %d " % tuple(int(x) for x in fi)
+        a = int(self.first[q])
+        for k in range(s.maxcoin):
+            line += "%d " % int(self.fra[a + k])
+        return line + "\n"
+
+    def coi_bytes(self) -> bytes:
+        """The .coi file (coincidences.c:529-533): per record unsigned short w,
+        5 floats, w unsigned short frames, w int positions."""
+        import struct
+        out = bytearray()
+        for q in range(len(self.w)):
+            w = int(self.w[q])
+            out += struct.pack("<H", w)
+            out += np.asarray(self.mean[q], dtype=np.float64).astype("<f4").tobytes()
+            a, b = int(self.first[q]), int(self.first[q]) + w
+            out += np.asarray(self.fra[a:b], dtype="<u2").tobytes()
+            out += np.asarray(self.ops[a:b], dtype="<i4").tobytes()
+        return bytes(out)
+
+
+class Coinc:
+    """pa_coinc: the coincidence step on the device.  Frames are added in the
+    reference's directory order; run() returns a CoincResult."""
+
+    def __init__(self, cfg: CoincCfg):
+        self.lib = load()
+        st = C.c_int(0)
+        self.cc = self.lib.pa_coinc_create(C.byref(cfg), C.byref(st))
+        if not self.cc:
+            raise SearchError("pa_coinc_create failed (%d): %s" % (st.value, self.lib.pa_coinc_last_error(None).decode()))
+
+    def _check(self, rc, what):
+        if rc != PA_OK:
+            raise SearchError("%s failed (%d): %s" % (what, rc, self.lib.pa_coinc_last_error(self.cc).decode()))
+
+    def reset(self):
+        self._check(self.lib.pa_coinc_reset(self.cc), "pa_coinc_reset")
+
+    def add_frame(self, frame: int, records: np.ndarray):
+        r = np.ascontiguousarray(records, dtype=np.float64).reshape(-1, 5)
+        self._check(self.lib.pa_coinc_add_frame(self.cc, int(frame), _dp(r), len(r)), "pa_coinc_add_frame")
+
+    def run(self, cells: bool = False) -> CoincResult:
+        s = CoincSummary()
+        self._check(self.lib.pa_coinc_run(self.cc, C.byref(s)), "pa_coinc_run")
+        fi = np.zeros((max(1, s.nframes), 3), dtype=np.int32)
+        recs = (CoincRec * max(1, s.ncoin))()
+        fra = np.zeros(max(1, s.nmembers), dtype=np.int32)
+        ops = np.zeros(max(1, s.nmembers), dtype=np.int32)
+        IP = C.POINTER(C.c_int)
+        self._check(self.lib.pa_coinc_get(self.cc, fi.ctypes.data_as(IP), recs, fra.ctypes.data_as(IP),
+                                          ops.ctypes.data_as(IP)), "pa_coinc_get")
+        w = np.array([recs[q].w for q in range(s.ncoin)], dtype=np.int32)
+        first = np.array([recs[q].first for q in range(s.ncoin)], dtype=np.int64)
+        mean = np.array([list(recs[q].mean) for q in range(s.ncoin)], dtype=np.float64).reshape(-1, 5)
+        cl = kp = None
+        if cells:
+            cl = np.zeros((max(1, s.inband), 4), dtype=np.int32)
+            kp = np.zeros(max(1, s.inband), dtype=np.uint8)
+            self._check(self.lib.pa_coinc_cells(self.cc, cl.ctypes.data_as(IP), kp.ctypes.data_as(C.POINTER(C.c_ubyte))),
+                        "pa_coinc_cells")
+            cl, kp = cl[:s.inband], kp[:s.inband]
+        return CoincResult(s, fi[:s.nframes], w, first, mean, fra[:s.nmembers], ops[:s.nmembers], cl, kp)
+
+    def last_call_ms(self) -> float:
+        return self.lib.pa_coinc_last_call_ms(self.cc)
+
+    def launches(self) -> int:
+        return self.lib.pa_coinc_kernel_launches(self.cc)
+
+    def close(self):
+        if getattr(self, "cc", None):
+            self.lib.pa_coinc_destroy(self.cc)
+            self.cc = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -352,3 +352,129 @@ def inject(ds: Dataset, *, f: float, fdot: float, delta: float, alpha: float, sn
         x = np.where(x != 0.0, x + h0 * sig, x)
         x.astype("<f8").tofile(xp)
         ds.files[d + "/xdat"] = _sha(xp)
+
+
+# ---------------------------------------------------------------------------
+# Trigger files of several time frames, the input of the coincidence step
+# (coincidences/src/coincidences.c:117-330), and the reference grid.bin that
+# carries its Fisher matrix (init.c:1142-1172).
+# ---------------------------------------------------------------------------
+
+def fisher_matrix(N: int, oms: float, widths=(8.0, 16.0, 2.0e6, 2.0e6),
+                  angles=(0.3, 0.5)) -> np.ndarray:
+    """Symmetric positive-definite 4x4 matrix Q diag(1/w^2) Q^T (row-major)
+    acting on the linear coordinates (f N, s N^2, oms N be0, oms N be1) of
+    coincidences.c:251-263: cells are w wide along the columns of Q, two
+    Givens rotations (f with s, the two sky coordinates) by `angles`."""
+    del N, oms
+    s0, c0 = (float(v[0]) for v in det_sincos(np.array([angles[0]])))
+    s1, c1 = (float(v[0]) for v in det_sincos(np.array([angles[1]])))
+    Q = np.array([[c0, -s0, 0., 0.], [s0, c0, 0., 0.], [0., 0., c1, -s1], [0., 0., s1, c1]])
+    lam = np.array([1.0 / (w * w) for w in widths])
+    G = np.zeros((4, 4))
+    for i in range(4):
+        for j in range(4):
+            acc = 0.0
+            for k in range(4):
+                acc = acc + Q[i, k] * lam[k] * Q[j, k]
+            G[i, j] = acc
+    return G
+
+
+def write_coinc_grid(path: str, fisher: np.ndarray, fftpad: int = 1) -> str:
+    """grid.bin as the coincidence program reads it: int fftpad, the grid
+    generator (16 doubles, unused there), the Fisher matrix (16 doubles,
+    init.c:1162-1167), 16 filler doubles."""
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, "wb") as f:
+        f.write(struct.pack("<i", fftpad))
+        f.write(np.zeros(16, dtype="<f8").tobytes())
+        f.write(np.asarray(fisher, dtype="<f8").reshape(16).tobytes())
+        f.write(np.zeros(16, dtype="<f8").tobytes())
+    return _sha(path)
+
+
+def trigger_name(frame: int, band: int, hemi: int = 2) -> str:
+    """triggers_<frame>_<band><label>_<hemi>.bin (jobcore.c:92-93)."""
+    return "triggers_%03d_%04d_%d.bin" % (frame, band, hemi)
+
+
+def coinc_triggers(frames, per_frame: int, *, N: int, refr: int, seed: int = 7,
+                   lines: int = 6, sky: int = 12, signals: int = 24,
+                   f_lo: float = 0.3, f_hi: float = 2.8) -> dict:
+    """Deterministic trigger records [f, s, delta, alpha, snr] per frame.
+
+    A mix that exercises every branch of the coincidence step:
+    * lattice triggers: f on a few lines with a step of half a frequency
+      cell, s = 0 or a few spindown steps, sky from a small set, SNR from a
+      small set (exact duplicates within and across frames, SNR ties, values
+      under the SNR cut);
+    * continuous triggers near the same lines (random cells);
+    * signals: one record per frame whose f shifted to the reference frame
+      (f + 2 s N (refr - frame), coincidences.c:235) is the same for every
+      frame, so that they coincide;
+    * records outside the band and far outside the narrowed band.
+    Only exact uniforms and + - * / enter the values, so the files are
+    byte-identical on every IEEE-754 machine."""
+    frames = list(frames)
+    out = {}
+    step_f = 4.0 / N                       # half a frequency cell (width 8 in f N)
+    step_s = 8.0 / (float(N) * float(N))   # half a spindown cell (width 16 in s N^2)
+    uL = uniform32(seed, lines + 2 * sky + 6 * signals, stream=500)
+    fl = f_lo + (f_hi - f_lo) * uL[:lines]
+    sky_d = -1.3 + 2.6 * uL[lines:lines + sky]
+    sky_a = 6.2 * uL[lines + sky:lines + 2 * sky]
+    sg = uL[lines + 2 * sky:].reshape(signals, 6) if signals else np.zeros((0, 6))
+    sig_f = f_lo + (f_hi - f_lo) * sg[:, 0]
+    sig_s = (sg[:, 1] - 0.5) * 64.0 * step_s
+    sig_d = -1.3 + 2.6 * sg[:, 2]
+    sig_a = 6.2 * sg[:, 3]
+    snr_set = np.array([5.5, 6.5, 7.0, 7.0, 8.25, 9.0])
+    for k, fr in enumerate(frames):
+        n_lat = per_frame // 2
+        n_con = per_frame - n_lat
+        u = uniform32(seed * 1000 + fr, 6 * per_frame + 4 * signals + 8, stream=501)
+        pos = [0]
+
+        def take(m, u=u, pos=pos):
+            pos[0] += m
+            return u[pos[0] - m:pos[0]]
+        a = take(n_lat)
+        li = np.floor(a * lines).astype(np.int64)
+        fj = np.floor(take(n_lat) * 9.0) - 4.0
+        f_lat = fl[li] + fj * step_f
+        s_lat = np.floor(take(n_lat) * 3.0) * step_s * 2.0 - 2.0 * step_s
+        si = np.floor(take(n_lat) * sky).astype(np.int64)
+        snr_lat = snr_set[np.floor(take(n_lat) * snr_set.size).astype(np.int64)]
+        li2 = np.floor(take(n_con) * lines).astype(np.int64)
+        f_con = fl[li2] + (take(n_con) - 0.5) * 40.0 * step_f
+        s_con = (take(n_con) - 0.5) * 16.0 * step_s
+        si2 = np.floor(take(n_con) * sky).astype(np.int64)
+        snr_con = 4.0 + 6.0 * take(n_con)
+        rec = [np.stack([f_lat, s_lat, sky_d[si], sky_a[si], snr_lat], axis=1),
+               np.stack([f_con, s_con, sky_d[si2] + (take(n_con) - 0.5) * 1e-4,
+                         sky_a[si2] + (take(n_con) - 0.5) * 1e-4, snr_con], axis=1)]
+        if signals:
+            present = take(signals) < 0.8
+            js = np.nonzero(present)[0]
+            fs = sig_f[js] - 2.0 * sig_s[js] * N * (refr - fr)
+            rec.append(np.stack([fs, sig_s[js], sig_d[js], sig_a[js], 7.0 + 3.0 * sg[js, 4]], axis=1))
+        # outside the band (shift pushes below 0) and outside a narrowed band
+        rec.append(np.array([[1e-7, 1e-9, 0.1, 0.2, 8.0], [0.05, 0.0, 0.3, 0.4, 9.0],
+                             [3.1, 0.0, -0.2, 5.0, 9.5]]))
+        r = np.concatenate(rec, axis=0)
+        order = np.argsort(uniform32(seed * 7 + fr, r.shape[0], stream=502), kind="stable")
+        out[fr] = np.ascontiguousarray(r[order])
+    return out
+
+
+def write_triggers(root: str, recs: dict, band: int = 666) -> dict:
+    """Writes each frame's records as little-endian doubles, 5 per record
+    (the search's trigger-file layout, jobcore.c:141).  Returns name -> sha256."""
+    os.makedirs(root, exist_ok=True)
+    files = {}
+    for fr, r in recs.items():
+        p = os.path.join(root, trigger_name(fr, band))
+        np.asarray(r, dtype="<f8").tofile(p)
+        files[os.path.basename(p)] = _sha(p)
+    return files

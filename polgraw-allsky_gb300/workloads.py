@@ -221,3 +221,22 @@ def segments(nseg: int = 24, *, nsky: int = 300, nspin: int = 150, seed: int = 2
         r.sst = 0
         out.append(dict(N=N, settings=s, dets=dets, keep=keep, tasks=tasks, opts=o, range=r))
     return out
+
+
+def coincidences(frames: int = 24, per_frame: int = 1 << 20, seed: int = 31) -> dict:
+    """Coincidence workload: trigger records of `frames` frames (segments
+    1..frames, reference frame in the middle), N = 86164 (2 days at dt = 2 s)
+    band 666, spread over 64 frequency lines x 256 sky positions with 1000
+    signals present in most frames; cells from the grid Fisher matrix of
+    synth.fisher_matrix.  Returns the settings, the records per frame and
+    the pa_coinc_cfg inputs (mincoin 4, no shift/scale, default cuts)."""
+    from . import synth
+    nod, dt, band = 2, 2.0, 666
+    N = synth.nsamples(nod, dt)
+    fpo = synth.fpo_default(band, dt)
+    oms = 2. * math.pi * fpo * dt
+    refr = (frames + 1) // 2
+    fr = list(range(1, frames + 1))
+    recs = synth.coinc_triggers(fr, per_frame, N=N, refr=refr, seed=seed, lines=64, sky=256, signals=1000)
+    return dict(N=N, fpo=fpo, oms=oms, refr=refr, frames=fr, recs=recs, fisher=synth.fisher_matrix(N, oms),
+                mincoin=4, band=band)

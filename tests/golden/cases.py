@@ -67,3 +67,29 @@ FOLLOWUP_CASES = [
          inject=dict(f=1.0, fdot=-6e-8, delta=0.3, alpha=1.2, snr=25.0),
          range=[0, 0, 0, 0, 0, 0, None, None]),
 ]
+
+# Coincidence step (coincidences/src/coincidences.c) over synthetic trigger
+# files of several frames (polgraw_gb300.synth.coinc_triggers) and a grid.bin
+# with a Fisher matrix (synth.fisher_matrix).  make_coinc_golden.py runs the
+# reference coincidence program built from its own sources
+# (oracle/_ref/coincidences-ref) and records its .coi file, its stderr line
+# and the directory order it read the frames in.
+#   coinc_basic       defaults (mincoin 3, no shift/scale, narrowdown 0.5)
+#   coinc_shift_scale cell shifts and scaling digits (coincidences.c:157-184),
+#                     mincoin 2, narrowed band, higher SNR cut
+#   coinc_quirks      crafted frames: SNR ties, a run whose best member is the
+#                     frame's first record (index 0 doubles as the "no run"
+#                     flag), frames whose last run meets the row left over from
+#                     an earlier frame, and a coincidence in the last cell of
+#                     the sorted table (written with multiplicity 0)
+#   coinc_many        24 frames x 5000 records, mincoin 4
+COINC_CASES = [
+    dict(name="coinc_basic", nod=2, dt=2.0, band=666, frames=[1, 2, 3, 5, 8, 9], per_frame=2000, seed=7,
+         refr=3, mincoin=3, shift=0, scale=1111, narrowdown=0.5, snrcutoff=6.0),
+    dict(name="coinc_shift_scale", nod=2, dt=2.0, band=666, frames=[2, 4, 6, 7], per_frame=1500, seed=11,
+         refr=4, mincoin=2, shift=1011, scale=2412, narrowdown=0.3, snrcutoff=6.5),
+    dict(name="coinc_quirks", nod=2, dt=2.0, band=666, frames=[1, 2, 3, 4, 5, 6], per_frame=160, seed=5,
+         refr=2, mincoin=3, shift=0, scale=1111, narrowdown=0.5, snrcutoff=6.0, craft=True),
+    dict(name="coinc_many", nod=2, dt=2.0, band=666, frames=list(range(1, 25)), per_frame=5000, seed=3,
+         refr=12, mincoin=4, shift=0, scale=1111, narrowdown=0.5, snrcutoff=6.0),
+]

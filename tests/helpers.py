@@ -78,3 +78,39 @@ def compare_candidates(ref_keys, ref_F, got_keys, got_F, trl, rtol):
 
 def snr_to_F(snr: np.ndarray, nd: int = 2) -> np.ndarray:
     return snr * snr / 2.0 + nd
+
+
+def parse_coi(b: bytes) -> list:
+    """Records of a .coi file (coincidences.c:529-533): (w, 5 floats, frames,
+    positions)."""
+    import struct
+    out, o = [], 0
+    while o < len(b):
+        w = struct.unpack_from("<H", b, o)[0]
+        o += 2
+        m = np.frombuffer(b[o:o + 20], dtype="<f4").copy()
+        o += 20
+        fra = np.frombuffer(b[o:o + 2 * w], dtype="<u2").copy()
+        o += 2 * w
+        ops = np.frombuffer(b[o:o + 4 * w], dtype="<i4").copy()
+        o += 4 * w
+        out.append((w, m, fra, ops))
+    return out
+
+
+def canon_coi(b: bytes) -> bytes:
+    """The .coi bytes with every NaN mean written as 0x7fc00000: the
+    multiplicity-0 record's means are 0/0, whose sign bit is the machine's
+    (set on x86-64, clear on aarch64)."""
+    out = bytearray(b)
+    o = 0
+    import struct
+    while o < len(b):
+        w = struct.unpack_from("<H", b, o)[0]
+        for k in range(5):
+            p = o + 2 + 4 * k
+            v = np.frombuffer(b[p:p + 4], dtype="<f4")[0]
+            if np.isnan(v):
+                out[p:p + 4] = struct.pack("<I", 0x7FC00000)
+        o += 22 + 6 * w
+    return bytes(out)
