@@ -430,6 +430,7 @@ def run_coinc(args, L):
     for _ in range(args.warmup):
         cc.run()
     l0 = cc.launches()
+    cc.set_profiling(True)
     clocks = ClockSampler(0)
     ms = 0.0
     for _ in range(args.steps):
@@ -437,8 +438,24 @@ def run_coinc(args, L):
         res = cc.run()
         ms += cc.last_call_ms()
     clk = clocks.stop()
+    prof = cc.profile()
+    cc.set_profiling(False)
     launches = (cc.launches() - l0) // max(1, args.steps)
     value = nrec * args.steps / (ms / 1e3)
+    # dominant kernel: the cells of every record (reads the 40-byte record,
+    # writes 16 bytes of cells and a 1-byte flag)
+    pk = peaks()
+    cells_ms, cells_n = prof["coinc_cells"]
+    per_launch = cells_ms / max(1, cells_n)
+    achieved = 57.0 * nrec / (per_launch / 1e3) / 1e9
+    tot = sum(v[0] for v in prof.values())
+    roof = {"bound": "hbm", "kernel": "coinc_cells", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"], "traffic": None,
+            "note": "57 B per record; the kernel is bound by the FP64 pipe (frequency and spindown terms and "
+                    "the rounding test in FP64, sky terms in FP32 with an FP64 recomputation near cell edges), "
+                    "not by HBM",
+            "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs)", "avg_launch_ms": per_launch,
+            "units_per_launch": nrec}
     # end to end: upload, run, results back
     t_e2e = 0.0
     for _ in range(args.steps):
@@ -480,6 +497,9 @@ def run_coinc(args, L):
             "cpu_baseline": {"value": nsub / t_cpu, "unit": "records/s", "cores": 1, "kind": "port",
                              "sample": "first %d records of each of the %d frames (CPU oracle, one thread, %.1f s)" %
                                        (args.coinc_cpu_records, len(frames), t_cpu)},
+            "roofline": roof,
+            "kernel_share": {k: round(v[0] / tot, 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])
+                             if v[1]},
             "matches_oracle_on_sample": bool(same)}
     cc.close()
     emit(line)

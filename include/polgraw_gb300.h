@@ -439,6 +439,11 @@ int pa_coinc_get(const pa_coinc *cc, int *frameinfo, pa_coinc_rec *recs, int *fr
 int pa_coinc_cells(const pa_coinc *cc, int *cells, unsigned char *keep);
 double pa_coinc_last_call_ms(const pa_coinc *cc);
 long long pa_coinc_kernel_launches(const pa_coinc *cc);
+/* Per-kernel profile of the following runs (CUDA events around every
+ * launch; resets the totals).  pa_coinc_profile_get: totals of kernel kind
+ * `kind` (0, 1, ...), PA_ERR_ARG past the last kind. */
+int pa_coinc_set_profiling(pa_coinc *cc, int on);
+int pa_coinc_profile_get(const pa_coinc *cc, int kind, const char **name, double *total_ms, long long *launches);
 
 #ifdef __cplusplus
 }

@@ -209,8 +209,6 @@ def coinc(cfg, frames, recs) -> "object":
         lib.ora_coinc_cells(o, cl.ctypes.data_as(IP), kp.ctypes.data_as(C.POINTER(C.c_ubyte)))
     finally:
         lib.ora_coinc_free(o)
-    w = np.array([rr[q].w for q in range(s.ncoin)], dtype=np.int32)
-    first = np.array([rr[q].first for q in range(s.ncoin)], dtype=np.int64)
-    mean = np.array([list(rr[q].mean) for q in range(s.ncoin)], dtype=np.float64).reshape(-1, 5)
+    w, first, mean = L.coinc_recs(rr, s.ncoin)
     return L.CoincResult(s, fi[:s.nframes], w, first, mean, fra[:s.nmembers], ops[:s.nmembers],
                          cl[:s.inband], kp[:s.inband])

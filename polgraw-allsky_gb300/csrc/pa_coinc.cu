@@ -71,6 +71,9 @@ struct CellArgs {
   double half_shift[4];    // 0.5 shift[j]
   int refr;
   double snrcut;
+  // FP32 sky terms: copies in float and, per cell column, the bound on
+  // |cell value (FP64) - cell value (FP32 sky terms)|
+  float omsN_f, se_f, ce_f, v2_f[4], v3_f[4], margin[4];
 };
 
 struct KeyLayout {
@@ -88,13 +91,26 @@ __device__ __forceinline__ int frame_of_block(int b) {
   return lo;
 }
 
-// coincidences.c:229-270 for one record; returns 1 when the record is kept
-__device__ __forceinline__ int cell_of(const double* __restrict__ r, double fshift, const CellArgs& a,
-                                      int4* cl) {
-  const double c0 = r[0], c1 = r[1], c2 = r[2], c3 = r[3], c4 = r[4];
-  if (!((c0 > a.lo) && (c0 < a.hi))) return 0;
-  const double c0s = __dadd_rn(c0, __dmul_rn(__dmul_rn(__dmul_rn(2., c1), a.N), fshift));
-  if (!(((c0s > 0) && (c0s < M_PI)) && (c4 > a.snrcut))) return 0;
+// frame of in-band record v: the last frame whose first in-band record is
+// <= v (empty frames share their successor's start); s_in = in_start in
+// shared memory
+__device__ __forceinline__ int frame_of_in(unsigned v, const unsigned* s_in, int nf) {
+  int lo = 0, hi = nf;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (s_in[mid] <= v) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void load_in_start(unsigned* s_in) {
+  for (int k = threadIdx.x; k <= c_ft.nframes; k += blockDim.x) s_in[k] = (unsigned)c_ft.in_start[k];
+  __syncthreads();
+}
+
+// coincidences.c:229-270 for one record in FP64, the reference's expression
+// order without contraction; the cells of the kept record in *cl
+__device__ __noinline__ void cells_f64(double c0s, double c1, double c2, double c3, const CellArgs& a, int4* cl) {
   double t[4];
   t[0] = __dmul_rn(c0s, a.N);
   t[1] = __dmul_rn(c1, a.sqrN);
@@ -114,6 +130,49 @@ __device__ __forceinline__ int cell_of(const double* __restrict__ r, double fshi
     s = __dadd_rn(s, __dmul_rn(t[3], a.v[3][j]));
     s = __dadd_rn(s, a.half_shift[j]);
     c[j] = (int)round(s);
+  }
+  *cl = make_int4(c[0], c[1], c[2], c[3]);
+}
+
+// Returns 1 when the record is kept.  GB300 runs FP64 at 1/64 of the FP32
+// rate, so the sky terms (two sincos, be0/be1 of ast2lin, auxi.c:34-35) are
+// first formed in FP32 and the frequency/spindown terms in FP64: the value
+// of each cell column then lies within a.margin[j] of the FP64 value (FP32
+// sincosf on |x| <= 8 with the argument rounded to float: <= 3.6e-7 per
+// sin/cos; the margin allows 8e-6 on be0 and be1).  When every column's
+// fractional part is farther than its margin from 1/2, both round to the
+// same integer; otherwise the record is recomputed in FP64.  The cells are
+// therefore those of the FP64 evaluation.
+__device__ __forceinline__ int cell_of(const double* __restrict__ r, double fshift, const CellArgs& a,
+                                      int4* cl) {
+  const double c0 = r[0], c1 = r[1], c2 = r[2], c3 = r[3], c4 = r[4];
+  if (!((c0 > a.lo) && (c0 < a.hi))) return 0;
+  const double c0s = __dadd_rn(c0, __dmul_rn(__dmul_rn(__dmul_rn(2., c1), a.N), fshift));
+  if (!(((c0s > 0) && (c0s < M_PI)) && (c4 > a.snrcut))) return 0;
+  const double t0 = __dmul_rn(c0s, a.N), t1 = __dmul_rn(c1, a.sqrN);
+  const float x3 = (float)c3, x2 = (float)c2;
+  bool exact = !(fabsf(x3) <= 8.f && fabsf(x2) <= 8.f);
+  int c[4];
+  if (!exact) {
+    float sa, ca, sd, cd;
+    sincosf(x3, &sa, &ca);
+    sincosf(x2, &sd, &cd);
+    const float be0 = fmaf(a.ce_f * sa, cd, a.se_f * sd);
+    const float be1 = ca * cd;
+    const float t2 = a.omsN_f * be0, t3 = a.omsN_f * be1;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      double s = fma(t0, a.v[0][j], fma(t1, a.v[1][j], a.half_shift[j]));
+      s += (double)fmaf(t2, a.v2_f[j], t3 * a.v3_f[j]);
+      const double fl = floor(s);
+      const float fr = (float)(s - fl);
+      exact |= fabsf(fr - 0.5f) <= a.margin[j];
+      c[j] = (int)fl + (fr > 0.5f ? 1 : 0);
+    }
+  }
+  if (exact) {
+    cells_f64(c0s, c1, c2, c3, a, cl);
+    return 1;
   }
   *cl = make_int4(c[0], c[1], c[2], c[3]);
   return 1;
@@ -249,8 +308,7 @@ template <typename K>
 __global__ void __launch_bounds__(kT) k_inband(const uint8_t* __restrict__ flag, const int4* __restrict__ cells_raw,
                                                const unsigned* __restrict__ blk_off, KeyLayout L,
                                                unsigned* __restrict__ rawidx, int4* __restrict__ cells_in,
-                                               uint8_t* __restrict__ fr_in, K* __restrict__ key,
-                                               unsigned* __restrict__ val) {
+                                               K* __restrict__ key, unsigned* __restrict__ val) {
   __shared__ unsigned sh[kT / 32];
   const int b = blockIdx.x;
   const int f = frame_of_block(b);
@@ -268,7 +326,6 @@ __global__ void __launch_bounds__(kT) k_inband(const uint8_t* __restrict__ flag,
       const int4 cl = cells_raw[r];
       rawidx[o] = (unsigned)r;
       cells_in[o] = cl;
-      fr_in[o] = (uint8_t)f;
       key[o] = make_key<K>(cl, L);
       val[o] = o;
     }
@@ -341,15 +398,17 @@ __global__ void __launch_bounds__(kT) k_radix_hist(const K* __restrict__ key, lo
 }
 
 // digit = frame of the element (for the per-frame ranks of the sorted order)
-__global__ void __launch_bounds__(kT) k_frame_hist(const unsigned* __restrict__ val, const uint8_t* __restrict__ fr_in,
-                                                   long long n, int nblk, unsigned* __restrict__ hist) {
+__global__ void __launch_bounds__(kT) k_frame_hist(const unsigned* __restrict__ val, long long n, int nblk,
+                                                   unsigned* __restrict__ hist) {
   __shared__ unsigned h[256];
+  __shared__ unsigned s_in[kMaxFrames + 1];
   h[threadIdx.x] = 0;
-  __syncthreads();
+  load_in_start(s_in);
+  const int nf = c_ft.nframes;
   const long long t0 = (long long)blockIdx.x * kRTile;
   for (int k = threadIdx.x; k < kRTile; k += kT) {
     const long long i = t0 + k;
-    if (i < n) atomicAdd(&h[fr_in[val[i]]], 1u);
+    if (i < n) atomicAdd(&h[frame_of_in(val[i], s_in, nf)], 1u);
   }
   __syncthreads();
   hist[(long long)threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
@@ -408,10 +467,13 @@ __global__ void __launch_bounds__(kT) k_radix_scatter(const K* __restrict__ kin,
 // frame's block offsets, then a count through the block's tile.
 template <typename K>
 __global__ void k_frame_find(const int2* __restrict__ req, int nreq, const unsigned* __restrict__ hoff, int nblk,
-                             const unsigned* __restrict__ val, const uint8_t* __restrict__ fr_in, long long n,
+                             const unsigned* __restrict__ val, long long n,
                              const K* __restrict__ key, const int4* __restrict__ cells_in,
                              long long* __restrict__ out, int4* __restrict__ out_cells,
                              unsigned long long* __restrict__ out_key) {
+  __shared__ unsigned s_in[kMaxFrames + 1];
+  load_in_start(s_in);
+  const int nf = c_ft.nframes;
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (r >= nreq) return;
@@ -429,7 +491,7 @@ __global__ void k_frame_find(const int2* __restrict__ req, int nreq, const unsig
   const long long t0 = (long long)lo * kRTile;
   for (int k = 0; k < kRTile; k += 32) {
     const long long i = t0 + k + lane;
-    const int hit = (i < n) && (fr_in[val[i]] == g);
+    const int hit = (i < n) && (frame_of_in(val[i], s_in, nf) == g);
     const unsigned bal = __ballot_sync(0xffffffffu, hit);
     const unsigned c = __popc(bal);
     if (need < c) {
@@ -454,26 +516,26 @@ __global__ void k_frame_find(const int2* __restrict__ req, int nreq, const unsig
 
 template <typename K>
 __global__ void __launch_bounds__(kT) k_dedup(const K* __restrict__ key, const unsigned* __restrict__ val,
-                                              const uint8_t* __restrict__ fr_in, const unsigned* __restrict__ rawidx,
-                                              const double* __restrict__ rec, long long n,
-                                              uint8_t* __restrict__ keep, uint8_t* __restrict__ keep_in,
-                                              unsigned* __restrict__ uniq) {
+                                              const unsigned* __restrict__ rawidx, const double* __restrict__ rec,
+                                              long long n, uint8_t* __restrict__ keep, unsigned* __restrict__ uniq) {
   __shared__ unsigned hcount[256];
+  __shared__ unsigned s_in[kMaxFrames + 1];
   hcount[threadIdx.x] = 0;
-  __syncthreads();
+  load_in_start(s_in);
+  const int nf = c_ft.nframes;
   const long long i = (long long)blockIdx.x * kT + threadIdx.x;
   if (i < n) {
     const K k0 = key[i];
     const unsigned v0 = val[i];
-    const int f = fr_in[v0];
+    const int f = frame_of_in(v0, s_in, nf);
     bool start = (i == 0);
-    if (!start) start = !(key[i - 1] == k0) || fr_in[val[i - 1]] != f;
+    if (!start) start = !(key[i - 1] == k0) || frame_of_in(val[i - 1], s_in, nf) != f;
     uint8_t kept = 0;
     if (start) {
-      const long long fs = c_ft.in_start[f];
+      const long long fs = s_in[f];
       // walk the run [i, j]
       long long j = i;
-      while (j + 1 < n && key[j + 1] == k0 && fr_in[val[j + 1]] == f) j++;
+      while (j + 1 < n && key[j + 1] == k0 && frame_of_in(val[j + 1], s_in, nf) == f) j++;
       // coincidences.c:317-413 over the pairs (t, t + 1) of the run
       long long maxsnridx = 0, maxi = i;
       double candsnr = 0;
@@ -495,9 +557,7 @@ __global__ void __launch_bounds__(kT) k_dedup(const K* __restrict__ key, const u
       }
       const bool dropped = c_ft.drop[f] && key_is(k0, c_ft.drop_lo[f], c_ft.drop_hi[f]);
       if (!dropped) {
-        const long long k = maxsnridx ? maxi : j;
-        keep[k] = 1;
-        keep_in[val[k]] = 1;
+        keep[maxsnridx ? maxi : j] = 1;
         kept = 1;
       }
     }
@@ -505,6 +565,13 @@ __global__ void __launch_bounds__(kT) k_dedup(const K* __restrict__ key, const u
   }
   __syncthreads();
   if (hcount[threadIdx.x]) atomicAdd(&uniq[threadIdx.x], hcount[threadIdx.x]);
+}
+
+// keep flags by in-band index, from the flags by sorted position
+__global__ void k_keep_scatter(const uint8_t* __restrict__ keep, const unsigned* __restrict__ val, long long n,
+                               uint8_t* __restrict__ keep_in) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) keep_in[val[i]] = keep[i];
 }
 
 // per-tile counts of a 0/1 array
@@ -603,8 +670,11 @@ __global__ void k_gather_w(const unsigned* __restrict__ order, const unsigned* _
 __global__ void k_means(const unsigned* __restrict__ order, const unsigned* __restrict__ cend,
                         const unsigned* __restrict__ cw, const unsigned* __restrict__ first, int K,
                         const unsigned* __restrict__ sval, const unsigned* __restrict__ rawidx,
-                        const uint8_t* __restrict__ fr_in, const double* __restrict__ rec, double N, int refr,
+                        const double* __restrict__ rec, double N, int refr,
                         double* __restrict__ mean, int* __restrict__ fra, int* __restrict__ ops) {
+  __shared__ unsigned s_in[kMaxFrames + 1];
+  load_in_start(s_in);
+  const int nf = c_ft.nframes;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= K) return;
   const unsigned g = order[q];
@@ -614,7 +684,7 @@ __global__ void k_means(const unsigned* __restrict__ order, const unsigned* __re
   double m[5] = {0, 0, 0, 0, 0};
   for (int i = 0; i < w; i++) {
     const unsigned v = sval[j - i];
-    const int f = fr_in[v];
+    const int f = frame_of_in(v, s_in, nf);
     const long long r = rawidx[v];
     const double* c = rec + 5 * r;
     const double fshift = (double)(refr - c_ft.frame_no[f]);
@@ -654,18 +724,64 @@ struct pa_coinc {
     void* p = nullptr;
     size_t n = 0;
   };
-  Buf rec, cells_raw, flag, blkcnt, scan_tmp, minmax, rawidx, cells_in, fr_in, keyA, keyB, valA, valB, hist,
+  Buf rec, cells_raw, flag, blkcnt, scan_tmp, minmax, rawidx, cells_in, keyA, keyB, valA, valB, hist,
       keep, keep_in, uniq, req, found, skey, sval, gflag, gend, gw, lastu, wkeyA, wkeyB, cend, cw, cidxA, cidxB,
       wsort, means, fra, ops;
+  // optional per-kernel profile: events around each launch while on
+  bool prof_on = false;
+  struct Open {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<Open> prof_open;
+  double prof_ms[16] = {0};
+  long long prof_n[16] = {0};
   // results
   pa_coinc_summary sum;
   std::vector<int> frameinfo;
   std::vector<pa_coinc_rec> recs;
   std::vector<int> h_fra, h_ops;
   long long n_in = 0;
+  const unsigned* val_sorted = nullptr;  // in-band index of each sorted position (last run)
 };
 
 static std::string g_coinc_create_error;
+
+enum CoincKind { CK_CELLS = 0, CK_INBAND, CK_SORT_HIST, CK_SORT_SCATTER, CK_SCAN, CK_FRAME_RANK, CK_DEDUP,
+                 CK_COMPACT, CK_GROUPS, CK_MEANS, CK_COUNT };
+static const char* const kCoincKindName[CK_COUNT] = {
+    "coinc_cells", "coinc_inband", "coinc_sort_hist", "coinc_sort_scatter", "coinc_scan",
+    "coinc_frame_rank", "coinc_dedup", "coinc_compact", "coinc_groups", "coinc_means"};
+
+// CUDA events around the launches of its scope, when profiling is on
+struct Span {
+  pa_coinc* c;
+  int kind;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Span(pa_coinc* c_, int k) : c(c_), kind(k) {
+    if (c->prof_on && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess)
+      cudaEventRecord(a, c->stream);
+  }
+  ~Span() {
+    if (a && b) {
+      cudaEventRecord(b, c->stream);
+      c->prof_open.push_back({kind, a, b});
+    }
+  }
+};
+
+static void prof_collect(pa_coinc* c) {
+  for (auto& o : c->prof_open) {
+    float ms = 0;
+    if (cudaEventSynchronize(o.b) == cudaSuccess && cudaEventElapsedTime(&ms, o.a, o.b) == cudaSuccess) {
+      c->prof_ms[o.kind] += ms;
+      c->prof_n[o.kind]++;
+    }
+    cudaEventDestroy(o.a);
+    cudaEventDestroy(o.b);
+  }
+  c->prof_open.clear();
+}
 
 static int cfail(pa_coinc* c, int code, const char* fmt, ...) {
   char buf[512];
@@ -713,12 +829,18 @@ static T* P(pa_coinc::Buf& b) { return (T*)b.p; }
 static int scan_excl(pa_coinc* c, unsigned* d, long long n, unsigned* tmp) {
   if (n <= 0) return PA_OK;
   const long long nb = (n + kTile - 1) / kTile;
-  k_scan_tiles<<<(unsigned)nb, kT, 0, c->stream>>>(d, n, nb > 1 ? tmp : nullptr);
+  {
+    Span sp_(c, CK_SCAN);
+    k_scan_tiles<<<(unsigned)nb, kT, 0, c->stream>>>(d, n, nb > 1 ? tmp : nullptr);
+  }
   c->launches++;
   if (nb > 1) {
     int rc = scan_excl(c, tmp, nb, tmp + nb);
     if (rc) return rc;
-    k_scan_add<<<(unsigned)nb, kT, 0, c->stream>>>(d, n, tmp);
+    {
+      Span sp_(c, CK_SCAN);
+      k_scan_add<<<(unsigned)nb, kT, 0, c->stream>>>(d, n, tmp);
+    }
     c->launches++;
   }
   CCK(cudaGetLastError(), "scan");
@@ -744,11 +866,17 @@ static int radix_sort(pa_coinc* c, K*& k, unsigned*& v, K* k2, unsigned* v2, lon
   K* kb = k2;
   unsigned* vb = v2;
   for (int s = 0; s < bits; s += 8) {
-    k_radix_hist<K><<<nblk, kT, 0, c->stream>>>(ka, n, s, nblk, P<unsigned>(c->hist));
+    {
+      Span sp_(c, CK_SORT_HIST);
+      k_radix_hist<K><<<nblk, kT, 0, c->stream>>>(ka, n, s, nblk, P<unsigned>(c->hist));
+    }
     c->launches++;
     int rc = scan_excl(c, P<unsigned>(c->hist), 256ll * nblk, P<unsigned>(c->scan_tmp));
     if (rc) return rc;
-    k_radix_scatter<K><<<nblk, kT, 0, c->stream>>>(ka, va, kb, vb, n, s, nblk, P<unsigned>(c->hist));
+    {
+      Span sp_(c, CK_SORT_SCATTER);
+      k_radix_scatter<K><<<nblk, kT, 0, c->stream>>>(ka, va, kb, vb, n, s, nblk, P<unsigned>(c->hist));
+    }
     c->launches++;
     CCK(cudaGetLastError(), "radix pass");
     K* tk = ka; ka = kb; kb = tk;
@@ -842,12 +970,16 @@ void pa_coinc_destroy(pa_coinc* c) {
   cudaSetDevice(c->cfg.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   pa_coinc::Buf* bufs[] = {&c->rec, &c->cells_raw, &c->flag, &c->blkcnt, &c->scan_tmp, &c->minmax, &c->rawidx,
-                           &c->cells_in, &c->fr_in, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->hist, &c->keep,
+                           &c->cells_in, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->hist, &c->keep,
                            &c->keep_in, &c->uniq, &c->req, &c->found, &c->skey, &c->sval, &c->gflag, &c->gend,
                            &c->gw, &c->lastu, &c->wkeyA, &c->wkeyB, &c->cend, &c->cw, &c->cidxA, &c->cidxB,
                            &c->wsort, &c->means, &c->fra, &c->ops};
   for (auto* b : bufs)
     if (b->p) cudaFree(b->p);
+  for (auto& o : c->prof_open) {
+    cudaEventDestroy(o.a);
+    cudaEventDestroy(o.b);
+  }
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -857,6 +989,7 @@ void pa_coinc_destroy(pa_coinc* c) {
 int pa_coinc_reset(pa_coinc* c) {
   if (!c) return PA_ERR_ARG;
   c->frames.clear();
+  c->val_sorted = nullptr;
   c->raw_start.assign(1, 0);
   c->nraw = 0;
   c->n_in = 0;
@@ -912,9 +1045,12 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
   ENS(keyB, sizeof(K) * n);
   ENS(valA, sizeof(unsigned) * n);
   ENS(valB, sizeof(unsigned) * n);
-  k_inband<K><<<nblk1, kT, 0, c->stream>>>(P<uint8_t>(c->flag), P<int4>(c->cells_raw), P<unsigned>(c->blkcnt), L,
-                                           P<unsigned>(c->rawidx), P<int4>(c->cells_in), P<uint8_t>(c->fr_in),
-                                           P<K>(c->keyA), P<unsigned>(c->valA));
+  {
+    Span sp_(c, CK_INBAND);
+    k_inband<K><<<nblk1, kT, 0, c->stream>>>(P<uint8_t>(c->flag), P<int4>(c->cells_raw), P<unsigned>(c->blkcnt), L,
+                                             P<unsigned>(c->rawidx), P<int4>(c->cells_in),
+                                             P<K>(c->keyA), P<unsigned>(c->valA));
+  }
   c->launches++;
   CCK(cudaGetLastError(), "k_inband");
   K* key = P<K>(c->keyA);
@@ -928,7 +1064,10 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
   const int nblkR = (int)((n + kRTile - 1) / kRTile);
   ENS(hist, sizeof(unsigned) * (256ll * nblkR + 1));
   ENS(scan_tmp, sizeof(unsigned) * scan_tmp_len(256ll * nblkR));
-  k_frame_hist<<<nblkR, kT, 0, c->stream>>>(val, P<uint8_t>(c->fr_in), n, nblkR, P<unsigned>(c->hist));
+  {
+    Span sp_(c, CK_FRAME_RANK);
+    k_frame_hist<<<nblkR, kT, 0, c->stream>>>(val, n, nblkR, P<unsigned>(c->hist));
+  }
   c->launches++;
   rc = scan_excl(c, P<unsigned>(c->hist), 256ll * nblkR, P<unsigned>(c->scan_tmp));
   if (rc) return rc;
@@ -960,9 +1099,12 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
     unsigned long long* d_keys = (unsigned long long*)(d_cells + nr);
     CCK(cudaMemcpyAsync(c->req.p, req.data(), sizeof(int2) * req.size(), cudaMemcpyHostToDevice, c->stream), "copy");
     const int wpb = kT / 32;
-    k_frame_find<K><<<(unsigned)((req.size() + wpb - 1) / wpb), kT, 0, c->stream>>>(
-        P<int2>(c->req), (int)req.size(), P<unsigned>(c->hist), nblkR, val, P<uint8_t>(c->fr_in), n, key,
-        P<int4>(c->cells_in), d_pos, d_cells, d_keys);
+    {
+      Span sp_(c, CK_FRAME_RANK);
+      k_frame_find<K><<<(unsigned)((req.size() + wpb - 1) / wpb), kT, 0, c->stream>>>(
+          P<int2>(c->req), (int)req.size(), P<unsigned>(c->hist), nblkR, val, n, key,
+          P<int4>(c->cells_in), d_pos, d_cells, d_keys);
+    }
     c->launches++;
     CCK(cudaGetLastError(), "k_frame_find");
     CCK(cudaMemcpyAsync(pos.data(), d_pos, sizeof(long long) * req.size(), cudaMemcpyDeviceToHost, c->stream), "copy");
@@ -990,22 +1132,26 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
 
   // duplicate removal
   ENS(keep, n);
-  ENS(keep_in, n);
   ENS(uniq, sizeof(unsigned) * 256);
   CCK(cudaMemsetAsync(c->keep.p, 0, n, c->stream), "memset");
-  CCK(cudaMemsetAsync(c->keep_in.p, 0, n, c->stream), "memset");
   CCK(cudaMemsetAsync(c->uniq.p, 0, sizeof(unsigned) * 256, c->stream), "memset");
-  k_dedup<K><<<(unsigned)((n + kT - 1) / kT), kT, 0, c->stream>>>(key, val, P<uint8_t>(c->fr_in),
-                                                                  P<unsigned>(c->rawidx), P<double>(c->rec), n,
-                                                                  P<uint8_t>(c->keep), P<uint8_t>(c->keep_in),
-                                                                  P<unsigned>(c->uniq));
+  c->val_sorted = val;
+  {
+    Span sp_(c, CK_DEDUP);
+    k_dedup<K><<<(unsigned)((n + kT - 1) / kT), kT, 0, c->stream>>>(key, val, P<unsigned>(c->rawidx),
+                                                                    P<double>(c->rec), n, P<uint8_t>(c->keep),
+                                                                    P<unsigned>(c->uniq));
+  }
   c->launches++;
   CCK(cudaGetLastError(), "k_dedup");
   // survivors in sorted order
   const long long nt = (n + kTile - 1) / kTile;
   ENS(blkcnt, sizeof(unsigned) * (nt + 1));
   ENS(scan_tmp, sizeof(unsigned) * scan_tmp_len(nt + 1));
-  k_tile_count<<<(unsigned)nt, kT, 0, c->stream>>>(P<uint8_t>(c->keep), n, P<unsigned>(c->blkcnt));
+  {
+    Span sp_(c, CK_COMPACT);
+    k_tile_count<<<(unsigned)nt, kT, 0, c->stream>>>(P<uint8_t>(c->keep), n, P<unsigned>(c->blkcnt));
+  }
   c->launches++;
   CCK(cudaMemsetAsync(P<unsigned>(c->blkcnt) + nt, 0, sizeof(unsigned), c->stream), "memset");
   rc = scan_excl(c, P<unsigned>(c->blkcnt), nt + 1, P<unsigned>(c->scan_tmp));
@@ -1020,8 +1166,11 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
   if (G == 0) return PA_OK;
   ENS(skey, sizeof(K) * G);
   ENS(sval, sizeof(unsigned) * G);
-  k_compact_surv<K><<<(unsigned)nt, kT, 0, c->stream>>>(P<uint8_t>(c->keep), n, P<unsigned>(c->blkcnt), key, val,
-                                                         P<K>(c->skey), P<unsigned>(c->sval));
+  {
+    Span sp_(c, CK_COMPACT);
+    k_compact_surv<K><<<(unsigned)nt, kT, 0, c->stream>>>(P<uint8_t>(c->keep), n, P<unsigned>(c->blkcnt), key, val,
+                                                           P<K>(c->skey), P<unsigned>(c->sval));
+  }
   c->launches++;
   CCK(cudaGetLastError(), "k_compact_surv");
 
@@ -1031,14 +1180,20 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
   ENS(gw, sizeof(unsigned) * G);
   ENS(lastu, sizeof(int));
   CCK(cudaMemsetAsync(c->lastu.p, 0, sizeof(int), c->stream), "memset");
-  k_groups<K><<<(G + kT - 1) / kT, kT, 0, c->stream>>>(P<K>(c->skey), G, c->cfg.mincoin, P<uint8_t>(c->gflag),
-                                                      P<unsigned>(c->gend), P<unsigned>(c->gw), P<int>(c->lastu));
+  {
+    Span sp_(c, CK_GROUPS);
+    k_groups<K><<<(G + kT - 1) / kT, kT, 0, c->stream>>>(P<K>(c->skey), G, c->cfg.mincoin, P<uint8_t>(c->gflag),
+                                                        P<unsigned>(c->gend), P<unsigned>(c->gw), P<int>(c->lastu));
+  }
   c->launches++;
   CCK(cudaGetLastError(), "k_groups");
   const long long gt = ((long long)G + kTile - 1) / kTile;
   ENS(blkcnt, sizeof(unsigned) * (gt + 1));
   ENS(scan_tmp, sizeof(unsigned) * scan_tmp_len(gt + 1));
-  k_tile_count<<<(unsigned)gt, kT, 0, c->stream>>>(P<uint8_t>(c->gflag), G, P<unsigned>(c->blkcnt));
+  {
+    Span sp_(c, CK_GROUPS);
+    k_tile_count<<<(unsigned)gt, kT, 0, c->stream>>>(P<uint8_t>(c->gflag), G, P<unsigned>(c->blkcnt));
+  }
   c->launches++;
   CCK(cudaMemsetAsync(P<unsigned>(c->blkcnt) + gt, 0, sizeof(unsigned), c->stream), "memset");
   rc = scan_excl(c, P<unsigned>(c->blkcnt), gt + 1, P<unsigned>(c->scan_tmp));
@@ -1057,10 +1212,13 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
     ENS(cw, sizeof(unsigned) * Kc);
     ENS(cidxA, sizeof(unsigned) * Kc);
     ENS(cidxB, sizeof(unsigned) * Kc);
-    k_compact_groups<<<(unsigned)gt, kT, 0, c->stream>>>(P<uint8_t>(c->gflag), G, P<unsigned>(c->blkcnt),
-                                                        P<unsigned>(c->gend), P<unsigned>(c->gw),
-                                                        P<unsigned long long>(c->wkeyA), P<unsigned>(c->cend),
-                                                        P<unsigned>(c->cw), P<unsigned>(c->cidxA));
+    {
+      Span sp_(c, CK_GROUPS);
+      k_compact_groups<<<(unsigned)gt, kT, 0, c->stream>>>(P<uint8_t>(c->gflag), G, P<unsigned>(c->blkcnt),
+                                                          P<unsigned>(c->gend), P<unsigned>(c->gw),
+                                                          P<unsigned long long>(c->wkeyA), P<unsigned>(c->cend),
+                                                          P<unsigned>(c->cw), P<unsigned>(c->cidxA));
+    }
     c->launches++;
     CCK(cudaGetLastError(), "k_compact_groups");
     // multiplicity descending, stable (coincidences.c:486)
@@ -1071,7 +1229,10 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
     // member offsets
     ENS(wsort, sizeof(unsigned) * (Kc + 1));
     ENS(scan_tmp, sizeof(unsigned) * scan_tmp_len(Kc + 1));
-    k_gather_w<<<(Kc + kT - 1) / kT, kT, 0, c->stream>>>(order, P<unsigned>(c->cw), (int)Kc, P<unsigned>(c->wsort));
+    {
+      Span sp_(c, CK_MEANS);
+      k_gather_w<<<(Kc + kT - 1) / kT, kT, 0, c->stream>>>(order, P<unsigned>(c->cw), (int)Kc, P<unsigned>(c->wsort));
+    }
     c->launches++;
     CCK(cudaMemsetAsync(P<unsigned>(c->wsort) + Kc, 0, sizeof(unsigned), c->stream), "memset");
     rc = scan_excl(c, P<unsigned>(c->wsort), (long long)Kc + 1, P<unsigned>(c->scan_tmp));
@@ -1082,11 +1243,14 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
     ENS(means, sizeof(double) * 5 * Kc);
     ENS(fra, sizeof(int) * (M + 1));
     ENS(ops, sizeof(int) * (M + 1));
-    k_means<<<(Kc + 127) / 128, 128, 0, c->stream>>>(order, P<unsigned>(c->cend), P<unsigned>(c->cw),
-                                                      P<unsigned>(c->wsort), (int)Kc, P<unsigned>(c->sval),
-                                                      P<unsigned>(c->rawidx), P<uint8_t>(c->fr_in), P<double>(c->rec),
-                                                      (double)c->cfg.N, c->cfg.refr, P<double>(c->means),
-                                                      P<int>(c->fra), P<int>(c->ops));
+    {
+      Span sp_(c, CK_MEANS);
+      k_means<<<(Kc + 127) / 128, 128, 0, c->stream>>>(order, P<unsigned>(c->cend), P<unsigned>(c->cw),
+                                                        P<unsigned>(c->wsort), (int)Kc, P<unsigned>(c->sval),
+                                                        P<unsigned>(c->rawidx), P<double>(c->rec),
+                                                        (double)c->cfg.N, c->cfg.refr, P<double>(c->means),
+                                                        P<int>(c->fra), P<int>(c->ops));
+    }
     c->launches++;
     CCK(cudaGetLastError(), "k_means");
     std::vector<unsigned> first(Kc), ws(Kc);
@@ -1146,6 +1310,7 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
   c->sum.nframes = nf;
   c->sum.raw = c->nraw;
   c->n_in = 0;
+  c->val_sorted = nullptr;
   CCK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
   // frame table
   memset(&c->ft, 0, sizeof(c->ft));
@@ -1178,6 +1343,17 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
     }
     a.refr = c->cfg.refr;
     a.snrcut = c->cfg.snrcutoff;
+    a.omsN_f = (float)a.omsN;
+    a.se_f = (float)a.se;
+    a.ce_f = (float)a.ce;
+    for (int j = 0; j < 4; j++) {
+      a.v2_f[j] = (float)a.v[2][j];
+      a.v3_f[j] = (float)a.v[3][j];
+      // 8e-6 on be0 and be1 (their FP32 error is below 1.1e-6), plus the
+      // FP32 products and the FP64 rounding differences
+      const double m = fabs(a.omsN) * (fabs(a.v[2][j]) + fabs(a.v[3][j])) * 8e-6 + 1e-6;
+      a.margin[j] = m < 1.0 ? (float)m : 1.0f;
+    }
     ENS(cells_raw, sizeof(int4) * c->nraw);
     ENS(flag, c->nraw);
     ENS(blkcnt, sizeof(unsigned) * (nblk1 + 1));
@@ -1185,8 +1361,11 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
     ENS(minmax, sizeof(int) * 8);
     const int mm0[8] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, INT_MIN};
     CCK(cudaMemcpyAsync(c->minmax.p, mm0, sizeof(mm0), cudaMemcpyHostToDevice, c->stream), "copy");
-    k_cells<<<nblk1, kT, 0, c->stream>>>(P<double>(c->rec), a, P<int4>(c->cells_raw), P<uint8_t>(c->flag),
-                                        P<unsigned>(c->blkcnt), P<int>(c->minmax));
+    {
+      Span sp_(c, CK_CELLS);
+      k_cells<<<nblk1, kT, 0, c->stream>>>(P<double>(c->rec), a, P<int4>(c->cells_raw), P<uint8_t>(c->flag),
+                                          P<unsigned>(c->blkcnt), P<int>(c->minmax));
+    }
     c->launches++;
     CCK(cudaGetLastError(), "k_cells");
     CCK(cudaMemsetAsync(P<unsigned>(c->blkcnt) + nblk1, 0, sizeof(unsigned), c->stream), "memset");
@@ -1210,7 +1389,6 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
     if (c->n_in > 0) {
       ENS(rawidx, sizeof(unsigned) * c->n_in);
       ENS(cells_in, sizeof(int4) * c->n_in);
-      ENS(fr_in, c->n_in);
       KeyLayout L;
       int bits[4], tot = 0;
       for (int j = 0; j < 4; j++) {
@@ -1243,6 +1421,7 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
   c->last_ms = ms;
+  prof_collect(c);
   if (sum) *sum = c->sum;
   return PA_OK;
 }
@@ -1263,12 +1442,40 @@ int pa_coinc_cells(const pa_coinc* cc, int* cells, unsigned char* keep) {
   CCK(cudaSetDevice(c->cfg.device), "cudaSetDevice");
   if (cells)
     CCK(cudaMemcpyAsync(cells, c->cells_in.p, sizeof(int4) * c->n_in, cudaMemcpyDeviceToHost, c->stream), "copy");
-  if (keep) CCK(cudaMemcpyAsync(keep, c->keep_in.p, c->n_in, cudaMemcpyDeviceToHost, c->stream), "copy");
+  if (keep) {
+    if (!c->val_sorted) return cfail(c, PA_ERR_ARG, "pa_coinc_cells: no completed run");
+    // keep flags by in-band index, from those by sorted position
+    int rc = ensure(c, c->keep_in, c->n_in);
+    if (rc) return rc;
+    k_keep_scatter<<<(unsigned)((c->n_in + kT - 1) / kT), kT, 0, c->stream>>>(P<uint8_t>(c->keep), c->val_sorted,
+                                                                               c->n_in, P<uint8_t>(c->keep_in));
+    c->launches++;
+    CCK(cudaGetLastError(), "k_keep_scatter");
+    CCK(cudaMemcpyAsync(keep, c->keep_in.p, c->n_in, cudaMemcpyDeviceToHost, c->stream), "copy");
+  }
   CCK(cudaStreamSynchronize(c->stream), "sync");
   return PA_OK;
 }
 
 double pa_coinc_last_call_ms(const pa_coinc* c) { return c ? c->last_ms : 0.0; }
+
+int pa_coinc_set_profiling(pa_coinc* c, int on) {
+  if (!c) return PA_ERR_ARG;
+  c->prof_on = on != 0;
+  for (int k = 0; k < CK_COUNT; k++) {
+    c->prof_ms[k] = 0;
+    c->prof_n[k] = 0;
+  }
+  return PA_OK;
+}
+
+int pa_coinc_profile_get(const pa_coinc* c, int kind, const char** name, double* total_ms, long long* launches) {
+  if (!c || kind < 0 || kind >= CK_COUNT) return PA_ERR_ARG;
+  if (name) *name = kCoincKindName[kind];
+  if (total_ms) *total_ms = c->prof_ms[kind];
+  if (launches) *launches = c->prof_n[kind];
+  return PA_OK;
+}
 long long pa_coinc_kernel_launches(const pa_coinc* c) { return c ? c->launches : 0; }
 
 }  // extern "C"

@@ -37,7 +37,7 @@ EXPORTS = [
     "pa_followup_ascent", "pa_followup_simplex", "pa_followup_last_call_ms", "pa_followup_kernel_launches",
     "pa_coinc_vedva", "pa_coinc_create", "pa_coinc_destroy", "pa_coinc_last_error", "pa_coinc_reset",
     "pa_coinc_add_frame", "pa_coinc_run", "pa_coinc_get", "pa_coinc_cells", "pa_coinc_last_call_ms",
-    "pa_coinc_kernel_launches", "pa_coinc_main",
+    "pa_coinc_kernel_launches", "pa_coinc_main", "pa_coinc_set_profiling", "pa_coinc_profile_get",
 ]
 
 
@@ -179,6 +179,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.pa_coinc_last_call_ms.argtypes = [C.c_void_p]
     lib.pa_coinc_kernel_launches.restype = C.c_longlong
     lib.pa_coinc_kernel_launches.argtypes = [C.c_void_p]
+    lib.pa_coinc_set_profiling.argtypes = [C.c_void_p, C.c_int]
+    lib.pa_coinc_profile_get.argtypes = [C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_longlong)]
     lib.pa_host_create.restype = C.c_void_p
     lib.pa_host_create.argtypes = [C.c_int, P(C.c_char_p), P(C.c_int)]
     lib.pa_host_setup.argtypes = [C.c_void_p]
@@ -676,6 +678,15 @@ def coinc_cfg(*, N: int, oms: float, vedva_m, shift: int = 0, scale: int = 1111,
     return c
 
 
+COINC_REC_DTYPE = np.dtype([("w", "<i4"), ("first", "<i4"), ("mean", "<f8", (5,))])
+
+
+def coinc_recs(recs, n: int):
+    """(w, first, mean[n, 5]) of a ctypes array of pa_coinc_rec."""
+    a = np.frombuffer(recs, dtype=COINC_REC_DTYPE, count=n) if n else np.zeros(0, dtype=COINC_REC_DTYPE)
+    return a["w"].astype(np.int32), a["first"].astype(np.int64), a["mean"].reshape(-1, 5).copy()
+
+
 class CoincResult:
     """Output of a coincidence run: per-frame counts, the records in file
     order (multiplicity w, FP64 means), and their members."""
@@ -756,9 +767,7 @@ class Coinc:
         IP = C.POINTER(C.c_int)
         self._check(self.lib.pa_coinc_get(self.cc, fi.ctypes.data_as(IP), recs, fra.ctypes.data_as(IP),
                                           ops.ctypes.data_as(IP)), "pa_coinc_get")
-        w = np.array([recs[q].w for q in range(s.ncoin)], dtype=np.int32)
-        first = np.array([recs[q].first for q in range(s.ncoin)], dtype=np.int64)
-        mean = np.array([list(recs[q].mean) for q in range(s.ncoin)], dtype=np.float64).reshape(-1, 5)
+        w, first, mean = coinc_recs(recs, s.ncoin)
         cl = kp = None
         if cells:
             cl = np.zeros((max(1, s.inband), 4), dtype=np.int32)
@@ -773,6 +782,19 @@ class Coinc:
 
     def launches(self) -> int:
         return self.lib.pa_coinc_kernel_launches(self.cc)
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.pa_coinc_set_profiling(self.cc, int(on)), "pa_coinc_set_profiling")
+
+    def profile(self) -> dict:
+        """{kernel kind: (total ms, launches)} since profiling was switched on."""
+        out, k = {}, 0
+        while True:
+            nm, ms, n = C.c_char_p(), C.c_double(), C.c_longlong()
+            if self.lib.pa_coinc_profile_get(self.cc, k, C.byref(nm), C.byref(ms), C.byref(n)) != PA_OK:
+                return out
+            out[nm.value.decode()] = (ms.value, n.value)
+            k += 1
 
     def close(self):
         if getattr(self, "cc", None):
