@@ -129,7 +129,7 @@ def l2_flush():
 # DRAM bytes (read + write) per spindown of the spindown pass A (H1+L1,
 # N=86164, nfftf=131072) from ncu captures of the kernel, per schedule
 # (spindowns per launch, FFT split); scaled by the spindowns of a launch
-PASS_A_TRAFFIC_PER_SPINDOWN = {(32, 0): 13.1e6 / 28.57, (64, 1): 79.02e6 / 64}
+PASS_A_TRAFFIC_PER_SPINDOWN = {(32, 0): 13.1e6 / 28.57, (64, 1): 79.02e6 / 64, (64, 0): 77.79e6 / 64}
 
 
 def peaks() -> dict:
@@ -489,6 +489,7 @@ def run_coinc(args, L):
             "config": {"workload": "%d frames x %d trigger records, N=86164, 64 lines x 256 sky, 1000 signals, "
                                    "mincoin 4" % (len(frames), args.coinc_records),
                        "records": nrec, "inband": int(s.inband), "unique": int(s.unique), "coincidences": int(s.ncoin),
+                       "fp64_cells": int(s.fp64_cells),
                        "maxcoin": int(s.maxcoin),
                        "l2": "flushed (256 MB write) before each timed step; records 1.0 GB > L2"},
             "clocks": clk, "gpu_launches": int(launches),

@@ -407,6 +407,8 @@ typedef struct pa_coinc_summary {
   long long nmembers;      /* sum of their multiplicities */
   int maxcoin;             /* largest multiplicity (0: none) */
   int maxcoin_index;       /* record with maxcoin and the largest mean SNR */
+  long long fp64_cells;    /* in-band records whose cells were recomputed in
+                              FP64 (near a rounding edge of the fast path) */
 } pa_coinc_summary;
 
 /* Host: vedva[i][j] = eigvec[i][j] sqrt(eigval[j]) of the symmetric 4x4

@@ -49,8 +49,7 @@ constexpr int kMaxFrames = 255;
 constexpr int kT = 256;                 // threads per block everywhere
 constexpr int kIt = 8;                  // items per thread (tiles of 2048)
 constexpr int kTile = kT * kIt;
-constexpr int kRChunks = 16;            // radix tile: 16 chunks of 256 items
-constexpr int kRTile = kT * kRChunks;
+constexpr int kRTile = 4096;            // radix tile (items per block)
 
 struct FrameTab {
   int nframes;
@@ -74,7 +73,35 @@ struct CellArgs {
   // FP32 sky terms: copies in float and, per cell column, the bound on
   // |cell value (FP64) - cell value (FP32 sky terms)|
   float omsN_f, se_f, ce_f, v2_f[4], v3_f[4], margin[4];
+  // float-float (hi + lo) copies for the frequency and spindown terms
+  float Nf, sqrN_h, sqrN_l, v0_h[4], v0_l[4], v1_h[4], v1_l[4], hs_f[4];
+  int fast;                // N < 2^24 (exact in float): the FP32/float-float path is on
 };
+
+// float-float arithmetic (hi + lo, about 44 significant bits): error-free
+// products by fmaf and sums by the two-sum of Knuth
+struct FF {
+  float h, l;
+};
+__device__ __forceinline__ FF ff_quick(float a, float b) {
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.h + b.h;
+  const float bb = s - a.h;
+  const float e = (a.h - (s - bb)) + (b.h - bb);
+  return ff_quick(s, e + (a.l + b.l));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = a.h * b.h;
+  const float e = fmaf(a.h, b.h, -p);
+  return ff_quick(p, fmaf(a.h, b.l, fmaf(a.l, b.h, e)));
+}
+__device__ __forceinline__ FF ff_of(double d) {
+  const float h = (float)d;
+  return {h, (float)(d - (double)h)};
+}
 
 struct KeyLayout {
   int maxc[4];             // column maxima
@@ -135,25 +162,29 @@ __device__ __noinline__ void cells_f64(double c0s, double c1, double c2, double 
 }
 
 // Returns 1 when the record is kept.  GB300 runs FP64 at 1/64 of the FP32
-// rate, so the sky terms (two sincos, be0/be1 of ast2lin, auxi.c:34-35) are
-// first formed in FP32 and the frequency/spindown terms in FP64: the value
-// of each cell column then lies within a.margin[j] of the FP64 value (FP32
-// sincosf on |x| <= 8 with the argument rounded to float: <= 3.6e-7 per
-// sin/cos; the margin allows 8e-6 on be0 and be1).  When every column's
-// fractional part is farther than its margin from 1/2, both round to the
-// same integer; otherwise the record is recomputed in FP64.  The cells are
-// therefore those of the FP64 evaluation.
+// rate, so only the frequency shift and the band/SNR tests (which must equal
+// the reference's comparisons) run in FP64; the cell values are first formed
+// with the frequency/spindown terms in float-float (about 44 bits) and the
+// sky terms (two sincos, be0/be1 of ast2lin, auxi.c:34-35) in FP32.  Each
+// column's value then lies within a.margin[j] + |value| 2^-36 of the FP64
+// value (FP32 sincosf on |x| <= 8 with the argument rounded to float: <= 3.6e-7
+// per sin/cos; the margin allows 8e-6 on be0 and be1).  When every column's
+// fractional part is farther than that from 1/2, both round to the same
+// integer; otherwise (or for |value| >= 2^22, or |delta|, |alpha| > 8) the
+// record is recomputed in FP64.  The cells are therefore those of the FP64
+// evaluation.
 __device__ __forceinline__ int cell_of(const double* __restrict__ r, double fshift, const CellArgs& a,
-                                      int4* cl) {
+                                      int4* cl, unsigned* nexact) {
   const double c0 = r[0], c1 = r[1], c2 = r[2], c3 = r[3], c4 = r[4];
   if (!((c0 > a.lo) && (c0 < a.hi))) return 0;
   const double c0s = __dadd_rn(c0, __dmul_rn(__dmul_rn(__dmul_rn(2., c1), a.N), fshift));
   if (!(((c0s > 0) && (c0s < M_PI)) && (c4 > a.snrcut))) return 0;
-  const double t0 = __dmul_rn(c0s, a.N), t1 = __dmul_rn(c1, a.sqrN);
   const float x3 = (float)c3, x2 = (float)c2;
-  bool exact = !(fabsf(x3) <= 8.f && fabsf(x2) <= 8.f);
+  bool exact = !a.fast || !(fabsf(x3) <= 8.f && fabsf(x2) <= 8.f);
   int c[4];
   if (!exact) {
+    const FF t0 = ff_mul(ff_of(c0s), FF{a.Nf, 0.f});
+    const FF t1 = ff_mul(ff_of(c1), FF{a.sqrN_h, a.sqrN_l});
     float sa, ca, sd, cd;
     sincosf(x3, &sa, &ca);
     sincosf(x2, &sd, &cd);
@@ -162,16 +193,28 @@ __device__ __forceinline__ int cell_of(const double* __restrict__ r, double fshi
     const float t2 = a.omsN_f * be0, t3 = a.omsN_f * be1;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      double s = fma(t0, a.v[0][j], fma(t1, a.v[1][j], a.half_shift[j]));
-      s += (double)fmaf(t2, a.v2_f[j], t3 * a.v3_f[j]);
-      const double fl = floor(s);
-      const float fr = (float)(s - fl);
-      exact |= fabsf(fr - 0.5f) <= a.margin[j];
+      FF v = ff_add(ff_mul(t0, FF{a.v0_h[j], a.v0_l[j]}), ff_mul(t1, FF{a.v1_h[j], a.v1_l[j]}));
+      v = ff_add(v, FF{a.hs_f[j], 0.f});
+      v = ff_add(v, FF{fmaf(t2, a.v2_f[j], t3 * a.v3_f[j]), 0.f});
+      float fl = floorf(v.h);
+      float fr = (v.h - fl) + v.l;
+      if (fr < 0.f) {
+        fl -= 1.f;
+        fr += 1.f;
+      } else if (fr >= 1.f) {
+        fl += 1.f;
+        fr -= 1.f;
+      }
+      // float-float rounding: below 2^-40 of the terms' magnitudes
+      const float av = fabsf(v.h);
+      const float terms = fabsf(t0.h * a.v0_h[j]) + fabsf(t1.h * a.v1_h[j]) + av;
+      exact |= !(av < 4194304.f) || fabsf(fr - 0.5f) <= a.margin[j] + terms * 1e-11f;
       c[j] = (int)fl + (fr > 0.5f ? 1 : 0);
     }
   }
   if (exact) {
     cells_f64(c0s, c1, c2, c3, a, cl);
+    atomicAdd(nexact, 1u);
     return 1;
   }
   *cl = make_int4(c[0], c[1], c[2], c[3]);
@@ -213,7 +256,8 @@ __device__ __forceinline__ unsigned block_flag_prefix(int flag, unsigned* sh, un
 
 __global__ void __launch_bounds__(kT) k_cells(const double* __restrict__ rec, CellArgs a,
                                               int4* __restrict__ cells_raw, uint8_t* __restrict__ flag,
-                                              unsigned* __restrict__ blk_cnt, int* __restrict__ minmax) {
+                                              unsigned* __restrict__ blk_cnt, int* __restrict__ minmax,
+                                              unsigned* __restrict__ nexact) {
   __shared__ unsigned sh[kT / 32];
   __shared__ int smm[8];
   const int b = blockIdx.x;
@@ -230,7 +274,7 @@ __global__ void __launch_bounds__(kT) k_cells(const double* __restrict__ rec, Ce
     const long long r = tile0 + (long long)it * kT + threadIdx.x;
     if (r >= fend) break;
     int4 cl = make_int4(0, 0, 0, 0);
-    const int ok = cell_of(rec + 5 * r, fshift, a, &cl);
+    const int ok = cell_of(rec + 5 * r, fshift, a, &cl, nexact);
     flag[r] = (uint8_t)ok;
     cells_raw[r] = cl;
     if (ok) {
@@ -414,36 +458,51 @@ __global__ void __launch_bounds__(kT) k_frame_hist(const unsigned* __restrict__ 
   hist[(long long)threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
 }
 
+// Stable scatter of one 8-bit digit.  A tile (kRTile items) is taken in
+// chunks of kT x kSub items, each thread holding kSub items (item j*kT + t
+// of the chunk), so that a chunk's loads are in flight together and its
+// four barriers serve kSub items per thread.  Ranks: peers with the same
+// digit in the warp (match_any), then an exclusive prefix per digit over the
+// (item slot, warp) pairs in item order.
+constexpr int kSub = 4;
+constexpr int kChunk = kT * kSub;
+constexpr int kSlots = kSub * (kT / 32);
 template <typename K>
 __global__ void __launch_bounds__(kT) k_radix_scatter(const K* __restrict__ kin, const unsigned* __restrict__ vin,
                                                       K* __restrict__ kout, unsigned* __restrict__ vout, long long n,
                                                       int shift, int nblk, const unsigned* __restrict__ off) {
-  __shared__ unsigned wc[kT / 32][256];
+  __shared__ unsigned wc[kSlots][256];
   __shared__ unsigned run[256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   run[threadIdx.x] = off[(long long)threadIdx.x * nblk + blockIdx.x];
   const long long t0 = (long long)blockIdx.x * kRTile;
-  for (int c = 0; c < kRChunks; c++) {
-    for (int k = 0; k < kT / 32; k++) wc[k][threadIdx.x] = 0;
-    __syncthreads();
-    const long long i = t0 + (long long)c * kT + threadIdx.x;
-    const bool valid = i < n;
-    K kk;
-    unsigned vv = 0, d = 256;
-    if (valid) {
-      kk = kin[i];
-      vv = vin[i];
-      d = digit_of(kk, shift);
+  for (int c = 0; c < kRTile / kChunk; c++) {
+    K kk[kSub];
+    unsigned vv[kSub], d[kSub], rank[kSub];
+#pragma unroll
+    for (int j = 0; j < kSub; j++) {
+      const long long i = t0 + (long long)c * kChunk + j * kT + threadIdx.x;
+      d[j] = 256;
+      vv[j] = 0;
+      if (i < n) {
+        kk[j] = kin[i];
+        vv[j] = vin[i];
+        d[j] = digit_of(kk[j], shift);
+      }
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    const unsigned rank = __popc(peers & ((1u << lane) - 1u));
-    const int leader = __ffs(peers) - 1;
-    if (valid && lane == leader) wc[w][d] = __popc(peers);
+    for (int k = 0; k < kSlots; k++) wc[k][threadIdx.x] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kSub; j++) {
+      const unsigned peers = __match_any_sync(0xffffffffu, d[j]);
+      rank[j] = __popc(peers & ((1u << lane) - 1u));
+      if (d[j] < 256 && lane == __ffs(peers) - 1) wc[j * (kT / 32) + w][d[j]] = __popc(peers);
+    }
     __syncthreads();
     {
       const int dg = threadIdx.x;
       unsigned p = run[dg];
-      for (int k = 0; k < kT / 32; k++) {
+      for (int k = 0; k < kSlots; k++) {
         const unsigned t = wc[k][dg];
         wc[k][dg] = p;
         p += t;
@@ -451,11 +510,13 @@ __global__ void __launch_bounds__(kT) k_radix_scatter(const K* __restrict__ kin,
       run[dg] = p;
     }
     __syncthreads();
-    if (valid) {
-      const unsigned pos = wc[w][d] + rank;
-      kout[pos] = kk;
-      vout[pos] = vv;
-    }
+#pragma unroll
+    for (int j = 0; j < kSub; j++)
+      if (d[j] < 256) {
+        const unsigned pos = wc[j * (kT / 32) + w][d[j]] + rank[j];
+        kout[pos] = kk[j];
+        vout[pos] = vv[j];
+      }
     __syncthreads();
   }
 }
@@ -671,7 +732,7 @@ __global__ void k_means(const unsigned* __restrict__ order, const unsigned* __re
                         const unsigned* __restrict__ cw, const unsigned* __restrict__ first, int K,
                         const unsigned* __restrict__ sval, const unsigned* __restrict__ rawidx,
                         const double* __restrict__ rec, double N, int refr,
-                        double* __restrict__ mean, int* __restrict__ fra, int* __restrict__ ops) {
+                        pa_coinc_rec* __restrict__ out, int* __restrict__ fra, int* __restrict__ ops) {
   __shared__ unsigned s_in[kMaxFrames + 1];
   load_in_start(s_in);
   const int nf = c_ft.nframes;
@@ -698,8 +759,12 @@ __global__ void k_means(const unsigned* __restrict__ order, const unsigned* __re
     fra[m0 + i] = c_ft.frame_no[f];
   }
   const double dw = (double)w;
-  for (int l = 0; l < 4; l++) mean[5 * (long long)q + l] = __ddiv_rn(m[l], dw);
-  mean[5 * (long long)q + 4] = __dsqrt_rn(m[4]);
+  pa_coinc_rec r;
+  r.w = w;
+  r.first = (int)m0;
+  for (int l = 0; l < 4; l++) r.mean[l] = __ddiv_rn(m[l], dw);
+  r.mean[4] = __dsqrt_rn(m[4]);
+  out[q] = r;
 }
 
 }  // namespace
@@ -739,8 +804,11 @@ struct pa_coinc {
   // results
   pa_coinc_summary sum;
   std::vector<int> frameinfo;
-  std::vector<pa_coinc_rec> recs;
-  std::vector<int> h_fra, h_ops;
+  // results in page-locked host memory (grow only)
+  pa_coinc_rec* h_recs = nullptr;
+  int* h_fra = nullptr;
+  int* h_ops = nullptr;
+  size_t h_recs_cap = 0, h_mem_cap = 0;
   long long n_in = 0;
   const unsigned* val_sorted = nullptr;  // in-band index of each sorted position (last run)
 };
@@ -980,6 +1048,9 @@ void pa_coinc_destroy(pa_coinc* c) {
     cudaEventDestroy(o.a);
     cudaEventDestroy(o.b);
   }
+  if (c->h_recs) cudaFreeHost(c->h_recs);
+  if (c->h_fra) cudaFreeHost(c->h_fra);
+  if (c->h_ops) cudaFreeHost(c->h_ops);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -995,9 +1066,7 @@ int pa_coinc_reset(pa_coinc* c) {
   c->n_in = 0;
   memset(&c->sum, 0, sizeof(c->sum));
   c->frameinfo.clear();
-  c->recs.clear();
-  c->h_fra.clear();
-  c->h_ops.clear();
+
   return PA_OK;
 }
 
@@ -1204,7 +1273,14 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
   CCK(cudaMemcpyAsync(&lastu, c->lastu.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "copy");
   CCK(cudaStreamSynchronize(c->stream), "sync");
   const int ncoin = (int)Kc + (lastu ? 1 : 0);
-  c->recs.assign(ncoin, pa_coinc_rec());
+  if ((size_t)ncoin + 1 > c->h_recs_cap) {
+    if (c->h_recs) cudaFreeHost(c->h_recs);
+    c->h_recs = nullptr;
+    c->h_recs_cap = 0;
+    const size_t cap = (size_t)ncoin + 1 + ncoin / 2;
+    CCK(cudaMallocHost((void**)&c->h_recs, sizeof(pa_coinc_rec) * cap), "cudaMallocHost");
+    c->h_recs_cap = cap;
+  }
   if (Kc > 0) {
     ENS(wkeyA, sizeof(unsigned long long) * Kc);
     ENS(wkeyB, sizeof(unsigned long long) * Kc);
@@ -1240,7 +1316,7 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
     unsigned M = 0;
     CCK(cudaMemcpyAsync(&M, P<unsigned>(c->wsort) + Kc, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream), "copy");
     CCK(cudaStreamSynchronize(c->stream), "sync");
-    ENS(means, sizeof(double) * 5 * Kc);
+    ENS(means, sizeof(pa_coinc_rec) * Kc);
     ENS(fra, sizeof(int) * (M + 1));
     ENS(ops, sizeof(int) * (M + 1));
     {
@@ -1248,34 +1324,35 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
       k_means<<<(Kc + 127) / 128, 128, 0, c->stream>>>(order, P<unsigned>(c->cend), P<unsigned>(c->cw),
                                                         P<unsigned>(c->wsort), (int)Kc, P<unsigned>(c->sval),
                                                         P<unsigned>(c->rawidx), P<double>(c->rec),
-                                                        (double)c->cfg.N, c->cfg.refr, P<double>(c->means),
+                                                        (double)c->cfg.N, c->cfg.refr, P<pa_coinc_rec>(c->means),
                                                         P<int>(c->fra), P<int>(c->ops));
     }
     c->launches++;
     CCK(cudaGetLastError(), "k_means");
-    std::vector<unsigned> first(Kc), ws(Kc);
-    std::vector<double> mean(5 * (size_t)Kc);
-    c->h_fra.resize(M);
-    c->h_ops.resize(M);
-    CCK(cudaMemcpyAsync(first.data(), c->wsort.p, sizeof(unsigned) * Kc, cudaMemcpyDeviceToHost, c->stream), "copy");
-    CCK(cudaMemcpyAsync(mean.data(), c->means.p, sizeof(double) * 5 * Kc, cudaMemcpyDeviceToHost, c->stream), "copy");
+    if ((size_t)M + 1 > c->h_mem_cap) {
+      if (c->h_fra) cudaFreeHost(c->h_fra);
+      if (c->h_ops) cudaFreeHost(c->h_ops);
+      c->h_fra = c->h_ops = nullptr;
+      c->h_mem_cap = 0;
+      const size_t cap = (size_t)M + 1 + M / 2;
+      CCK(cudaMallocHost((void**)&c->h_fra, sizeof(int) * cap), "cudaMallocHost");
+      CCK(cudaMallocHost((void**)&c->h_ops, sizeof(int) * cap), "cudaMallocHost");
+      c->h_mem_cap = cap;
+    }
+    CCK(cudaMemcpyAsync(c->h_recs, c->means.p, sizeof(pa_coinc_rec) * Kc, cudaMemcpyDeviceToHost, c->stream),
+        "copy");
     if (M) {
-      CCK(cudaMemcpyAsync(c->h_fra.data(), c->fra.p, sizeof(int) * M, cudaMemcpyDeviceToHost, c->stream), "copy");
-      CCK(cudaMemcpyAsync(c->h_ops.data(), c->ops.p, sizeof(int) * M, cudaMemcpyDeviceToHost, c->stream), "copy");
+      CCK(cudaMemcpyAsync(c->h_fra, c->fra.p, sizeof(int) * M, cudaMemcpyDeviceToHost, c->stream), "copy");
+      CCK(cudaMemcpyAsync(c->h_ops, c->ops.p, sizeof(int) * M, cudaMemcpyDeviceToHost, c->stream), "copy");
     }
     CCK(cudaStreamSynchronize(c->stream), "sync");
-    for (unsigned q = 0; q < Kc; q++) {
-      c->recs[q].first = (int)first[q];
-      c->recs[q].w = (int)((q + 1 < Kc ? first[q + 1] : M) - first[q]);
-      memcpy(c->recs[q].mean, &mean[5 * (size_t)q], sizeof(double) * 5);
-    }
     c->sum.nmembers = M;
   }
   if (lastu) {
     // the last group is counted but never stored: a record of multiplicity
     // 0 whose means are 0/0 (coincidences.c:504-512), computed at run time
     volatile double zero = 0.0;
-    pa_coinc_rec& r = c->recs[ncoin - 1];
+    pa_coinc_rec& r = c->h_recs[ncoin - 1];
     r.w = 0;
     r.first = (int)c->sum.nmembers;
     for (int l = 0; l < 4; l++) r.mean[l] = zero / zero;
@@ -1283,13 +1360,13 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
   }
   c->sum.ncoin = ncoin;
   // coincidences.c:535-541: the largest multiplicity with the largest SNR
-  c->sum.maxcoin = Kc > 0 ? c->recs[0].w : 0;
+  c->sum.maxcoin = Kc > 0 ? c->h_recs[0].w : 0;
   c->sum.maxcoin_index = 0;
   double maxsnr = 0;
   for (int q = 0; q < ncoin; q++) {
-    if (!q) maxsnr = c->recs[q].mean[4];
-    if (c->recs[q].w == c->sum.maxcoin && c->recs[q].mean[4] > maxsnr) {
-      maxsnr = c->recs[q].mean[4];
+    if (!q) maxsnr = c->h_recs[q].mean[4];
+    if (c->h_recs[q].w == c->sum.maxcoin && c->h_recs[q].mean[4] > maxsnr) {
+      maxsnr = c->h_recs[q].mean[4];
       c->sum.maxcoin_index = q;
     }
   }
@@ -1303,9 +1380,7 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
   CCK(cudaSetDevice(c->cfg.device), "cudaSetDevice");
   const int nf = (int)c->frames.size();
   memset(&c->sum, 0, sizeof(c->sum));
-  c->recs.clear();
-  c->h_fra.clear();
-  c->h_ops.clear();
+
   c->frameinfo.assign(3 * (size_t)nf, 0);
   c->sum.nframes = nf;
   c->sum.raw = c->nraw;
@@ -1346,25 +1421,36 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
     a.omsN_f = (float)a.omsN;
     a.se_f = (float)a.se;
     a.ce_f = (float)a.ce;
+    auto split = [](double d, float* h, float* l) {
+      *h = (float)d;
+      *l = (float)(d - (double)*h);
+    };
+    a.fast = c->cfg.N < (1 << 24);
+    a.Nf = (float)c->cfg.N;  // exact when fast
+    split(a.sqrN, &a.sqrN_h, &a.sqrN_l);
     for (int j = 0; j < 4; j++) {
+      split(a.v[0][j], &a.v0_h[j], &a.v0_l[j]);
+      split(a.v[1][j], &a.v1_h[j], &a.v1_l[j]);
+      a.hs_f[j] = (float)a.half_shift[j];  // exact: halves of digits
       a.v2_f[j] = (float)a.v[2][j];
       a.v3_f[j] = (float)a.v[3][j];
       // 8e-6 on be0 and be1 (their FP32 error is below 1.1e-6), plus the
       // FP32 products and the FP64 rounding differences
-      const double m = fabs(a.omsN) * (fabs(a.v[2][j]) + fabs(a.v[3][j])) * 8e-6 + 1e-6;
+      const double m = fabs(a.omsN) * (fabs(a.v[2][j]) + fabs(a.v[3][j])) * 8e-6 + 2e-6;
       a.margin[j] = m < 1.0 ? (float)m : 1.0f;
     }
     ENS(cells_raw, sizeof(int4) * c->nraw);
     ENS(flag, c->nraw);
     ENS(blkcnt, sizeof(unsigned) * (nblk1 + 1));
     ENS(scan_tmp, sizeof(unsigned) * scan_tmp_len(nblk1 + 1));
-    ENS(minmax, sizeof(int) * 8);
-    const int mm0[8] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, INT_MIN};
+    ENS(minmax, sizeof(int) * 9);
+    const int mm0[9] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, INT_MIN, 0};
     CCK(cudaMemcpyAsync(c->minmax.p, mm0, sizeof(mm0), cudaMemcpyHostToDevice, c->stream), "copy");
     {
       Span sp_(c, CK_CELLS);
       k_cells<<<nblk1, kT, 0, c->stream>>>(P<double>(c->rec), a, P<int4>(c->cells_raw), P<uint8_t>(c->flag),
-                                          P<unsigned>(c->blkcnt), P<int>(c->minmax));
+                                          P<unsigned>(c->blkcnt), P<int>(c->minmax),
+                                          (unsigned*)(P<int>(c->minmax) + 8));
     }
     c->launches++;
     CCK(cudaGetLastError(), "k_cells");
@@ -1372,7 +1458,7 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
     rc = scan_excl(c, P<unsigned>(c->blkcnt), nblk1 + 1, P<unsigned>(c->scan_tmp));
     if (rc) return rc;
     std::vector<unsigned> boff(nblk1 + 1);
-    int mm[8];
+    int mm[9];
     CCK(cudaMemcpyAsync(boff.data(), c->blkcnt.p, sizeof(unsigned) * (nblk1 + 1), cudaMemcpyDeviceToHost, c->stream),
         "copy");
     CCK(cudaMemcpyAsync(mm, c->minmax.p, sizeof(mm), cudaMemcpyDeviceToHost, c->stream), "copy");
@@ -1386,6 +1472,7 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
     }
     c->ft.in_start[nf] = c->n_in;
     c->sum.inband = c->n_in;
+    c->sum.fp64_cells = (unsigned)mm[8];
     if (c->n_in > 0) {
       ENS(rawidx, sizeof(unsigned) * c->n_in);
       ENS(cells_in, sizeof(int4) * c->n_in);
@@ -1429,9 +1516,9 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
 int pa_coinc_get(const pa_coinc* c, int* frameinfo, pa_coinc_rec* recs, int* fra, int* ops) {
   if (!c) return PA_ERR_ARG;
   if (frameinfo && !c->frameinfo.empty()) memcpy(frameinfo, c->frameinfo.data(), sizeof(int) * c->frameinfo.size());
-  if (recs && !c->recs.empty()) memcpy(recs, c->recs.data(), sizeof(pa_coinc_rec) * c->recs.size());
-  if (fra && !c->h_fra.empty()) memcpy(fra, c->h_fra.data(), sizeof(int) * c->h_fra.size());
-  if (ops && !c->h_ops.empty()) memcpy(ops, c->h_ops.data(), sizeof(int) * c->h_ops.size());
+  if (recs && c->sum.ncoin > 0) memcpy(recs, c->h_recs, sizeof(pa_coinc_rec) * c->sum.ncoin);
+  if (fra && c->sum.nmembers > 0) memcpy(fra, c->h_fra, sizeof(int) * c->sum.nmembers);
+  if (ops && c->sum.nmembers > 0) memcpy(ops, c->h_ops, sizeof(int) * c->sum.nmembers);
   return PA_OK;
 }
 

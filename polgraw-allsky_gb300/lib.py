@@ -88,7 +88,8 @@ class CoincRec(C.Structure):
 
 class CoincSummary(C.Structure):
     _fields_ = [("nframes", C.c_int), ("raw", C.c_longlong), ("inband", C.c_longlong), ("unique", C.c_longlong),
-                ("ncoin", C.c_int), ("nmembers", C.c_longlong), ("maxcoin", C.c_int), ("maxcoin_index", C.c_int)]
+                ("ncoin", C.c_int), ("nmembers", C.c_longlong), ("maxcoin", C.c_int), ("maxcoin_index", C.c_int),
+                ("fp64_cells", C.c_longlong)]
 
 
 _lib = None
