@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(kT) k_scan_add(unsigned* __restrict__ d, long 
 
 template <typename K>
 __global__ void __launch_bounds__(kT) k_radix_hist(const K* __restrict__ key, long long n, int shift, int nblk,
-                                                   unsigned* __restrict__ hist) {
+                                                   unsigned* __restrict__ hist, unsigned* __restrict__ cnt_local) {
   __shared__ unsigned h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -439,6 +439,7 @@ __global__ void __launch_bounds__(kT) k_radix_hist(const K* __restrict__ key, lo
   }
   __syncthreads();
   hist[(long long)threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
+  cnt_local[(long long)blockIdx.x * 256 + threadIdx.x] = h[threadIdx.x];
 }
 
 // digit = frame of the element (for the per-frame ranks of the sorted order)
@@ -458,53 +459,99 @@ __global__ void __launch_bounds__(kT) k_frame_hist(const unsigned* __restrict__ 
   hist[(long long)threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
 }
 
-// Stable scatter of one 8-bit digit.  A tile (kRTile items) is taken in
-// chunks of kT x kSub items, each thread holding kSub items (item j*kT + t
-// of the chunk), so that a chunk's loads are in flight together and its
-// four barriers serve kSub items per thread.  Ranks: peers with the same
-// digit in the warp (match_any), then an exclusive prefix per digit over the
-// (item slot, warp) pairs in item order.
-constexpr int kSub = 4;
+// Stable scatter of one 8-bit digit.  A tile of kRTile items is ranked in
+// chunks of kT x kSub items (item j*kT + t of a chunk held by thread t):
+// peers with the same digit in the warp (match_any), then an exclusive prefix
+// per digit over the (item slot, warp) pairs in item order, carried across
+// chunks.  Each item is staged in shared memory at its digit's place in the
+// tile (tile base from the tile's own digit counts), and the tile is then
+// written out digit run by digit run, so that consecutive threads store to
+// consecutive addresses.
+constexpr int kSub = 2;
 constexpr int kChunk = kT * kSub;
 constexpr int kSlots = kSub * (kT / 32);
+
+template <typename K>
+constexpr size_t scatter_smem() {
+  return (size_t)kRTile * (sizeof(K) + sizeof(unsigned) + 1) + sizeof(unsigned) * 256 * (kSlots + 3);
+}
+
+__device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* scr) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) scr[w] = x;
+  __syncthreads();
+  unsigned before = 0;
+  for (int k = 0; k < w; k++) before += scr[k];
+  __syncthreads();
+  return before + x - v;
+}
+
 template <typename K>
 __global__ void __launch_bounds__(kT) k_radix_scatter(const K* __restrict__ kin, const unsigned* __restrict__ vin,
                                                       K* __restrict__ kout, unsigned* __restrict__ vout, long long n,
-                                                      int shift, int nblk, const unsigned* __restrict__ off) {
-  __shared__ unsigned wc[kSlots][256];
-  __shared__ unsigned run[256];
+                                                      int shift, int nblk, const unsigned* __restrict__ off,
+                                                      const unsigned* __restrict__ cnt_local) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ unsigned scr[kT / 32];
+  K* st_k = (K*)smem;
+  unsigned* st_v = (unsigned*)(st_k + kRTile);
+  unsigned* wc = st_v + kRTile;              // [kSlots][256]
+  unsigned* run = wc + kSlots * 256;
+  unsigned* base = run + 256;
+  unsigned* goff = base + 256;
+  uint8_t* st_d = (uint8_t*)(goff + 256);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  run[threadIdx.x] = off[(long long)threadIdx.x * nblk + blockIdx.x];
   const long long t0 = (long long)blockIdx.x * kRTile;
-  for (int c = 0; c < kRTile / kChunk; c++) {
-    K kk[kSub];
-    unsigned vv[kSub], d[kSub], rank[kSub];
+  const long long rem = n - t0;
+  const int tn = rem < kRTile ? (int)rem : kRTile;
+  const unsigned bt = block_excl_scan(cnt_local[(long long)blockIdx.x * 256 + threadIdx.x], scr);
+  base[threadIdx.x] = bt;
+  goff[threadIdx.x] = off[(long long)threadIdx.x * nblk + blockIdx.x];
+  run[threadIdx.x] = 0;
+  // the thread's items of the whole tile, loaded together
+  constexpr int kCh = kRTile / kChunk;
+  K kk[kCh][kSub];
+  unsigned vv[kCh][kSub];
+#pragma unroll
+  for (int c = 0; c < kCh; c++)
 #pragma unroll
     for (int j = 0; j < kSub; j++) {
-      const long long i = t0 + (long long)c * kChunk + j * kT + threadIdx.x;
-      d[j] = 256;
-      vv[j] = 0;
-      if (i < n) {
-        kk[j] = kin[i];
-        vv[j] = vin[i];
-        d[j] = digit_of(kk[j], shift);
+      const int li = c * kChunk + j * kT + threadIdx.x;
+      vv[c][j] = 0;
+      if (li < tn) {
+        kk[c][j] = kin[t0 + li];
+        vv[c][j] = vin[t0 + li];
       }
     }
-    for (int k = 0; k < kSlots; k++) wc[k][threadIdx.x] = 0;
+#pragma unroll
+  for (int c = 0; c < kCh; c++) {
+    unsigned d[kSub], rank[kSub];
+#pragma unroll
+    for (int j = 0; j < kSub; j++) {
+      const int li = c * kChunk + j * kT + threadIdx.x;
+      d[j] = li < tn ? digit_of(kk[c][j], shift) : 256u;
+    }
+    for (int k = 0; k < kSlots; k++) wc[k * 256 + threadIdx.x] = 0;
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < kSub; j++) {
       const unsigned peers = __match_any_sync(0xffffffffu, d[j]);
       rank[j] = __popc(peers & ((1u << lane) - 1u));
-      if (d[j] < 256 && lane == __ffs(peers) - 1) wc[j * (kT / 32) + w][d[j]] = __popc(peers);
+      if (d[j] < 256 && lane == __ffs(peers) - 1) wc[(j * (kT / 32) + w) * 256 + d[j]] = __popc(peers);
     }
     __syncthreads();
     {
       const int dg = threadIdx.x;
       unsigned p = run[dg];
       for (int k = 0; k < kSlots; k++) {
-        const unsigned t = wc[k][dg];
-        wc[k][dg] = p;
+        const unsigned t = wc[k * 256 + dg];
+        wc[k * 256 + dg] = p;
         p += t;
       }
       run[dg] = p;
@@ -513,11 +560,18 @@ __global__ void __launch_bounds__(kT) k_radix_scatter(const K* __restrict__ kin,
 #pragma unroll
     for (int j = 0; j < kSub; j++)
       if (d[j] < 256) {
-        const unsigned pos = wc[j * (kT / 32) + w][d[j]] + rank[j];
-        kout[pos] = kk[j];
-        vout[pos] = vv[j];
+        const unsigned lp = base[d[j]] + wc[(j * (kT / 32) + w) * 256 + d[j]] + rank[j];
+        st_k[lp] = kk[c][j];
+        st_v[lp] = vv[c][j];
+        st_d[lp] = (uint8_t)d[j];
       }
     __syncthreads();
+  }
+  for (int q = threadIdx.x; q < tn; q += kT) {
+    const unsigned dq = st_d[q];
+    const unsigned g = goff[dq] + ((unsigned)q - base[dq]);
+    kout[g] = st_k[q];
+    vout[g] = st_v[q];
   }
 }
 
@@ -789,7 +843,7 @@ struct pa_coinc {
     void* p = nullptr;
     size_t n = 0;
   };
-  Buf rec, cells_raw, flag, blkcnt, scan_tmp, minmax, rawidx, cells_in, keyA, keyB, valA, valB, hist,
+  Buf rec, cells_raw, flag, blkcnt, scan_tmp, minmax, rawidx, cells_in, cntl, keyA, keyB, valA, valB, hist,
       keep, keep_in, uniq, req, found, skey, sval, gflag, gend, gw, lastu, wkeyA, wkeyB, cend, cw, cidxA, cidxB,
       wsort, means, fra, ops;
   // optional per-kernel profile: events around each launch while on
@@ -928,7 +982,11 @@ template <typename K>
 static int radix_sort(pa_coinc* c, K*& k, unsigned*& v, K* k2, unsigned* v2, long long n, int bits) {
   const int nblk = (int)((n + kRTile - 1) / kRTile);
   ENS(hist, sizeof(unsigned) * (256ll * nblk + 1));
+  ENS(cntl, sizeof(unsigned) * 256ll * nblk);
   ENS(scan_tmp, sizeof(unsigned) * scan_tmp_len(256ll * nblk));
+  // the staged scatter needs more than the default 48 KB of shared memory
+  CCK(cudaFuncSetAttribute(k_radix_scatter<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scatter_smem<K>()),
+      "cudaFuncSetAttribute");
   K* ka = k;
   unsigned* va = v;
   K* kb = k2;
@@ -936,14 +994,15 @@ static int radix_sort(pa_coinc* c, K*& k, unsigned*& v, K* k2, unsigned* v2, lon
   for (int s = 0; s < bits; s += 8) {
     {
       Span sp_(c, CK_SORT_HIST);
-      k_radix_hist<K><<<nblk, kT, 0, c->stream>>>(ka, n, s, nblk, P<unsigned>(c->hist));
+      k_radix_hist<K><<<nblk, kT, 0, c->stream>>>(ka, n, s, nblk, P<unsigned>(c->hist), P<unsigned>(c->cntl));
     }
     c->launches++;
     int rc = scan_excl(c, P<unsigned>(c->hist), 256ll * nblk, P<unsigned>(c->scan_tmp));
     if (rc) return rc;
     {
       Span sp_(c, CK_SORT_SCATTER);
-      k_radix_scatter<K><<<nblk, kT, 0, c->stream>>>(ka, va, kb, vb, n, s, nblk, P<unsigned>(c->hist));
+      k_radix_scatter<K><<<nblk, kT, scatter_smem<K>(), c->stream>>>(ka, va, kb, vb, n, s, nblk,
+                                                                      P<unsigned>(c->hist), P<unsigned>(c->cntl));
     }
     c->launches++;
     CCK(cudaGetLastError(), "radix pass");
@@ -1038,7 +1097,7 @@ void pa_coinc_destroy(pa_coinc* c) {
   cudaSetDevice(c->cfg.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   pa_coinc::Buf* bufs[] = {&c->rec, &c->cells_raw, &c->flag, &c->blkcnt, &c->scan_tmp, &c->minmax, &c->rawidx,
-                           &c->cells_in, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->hist, &c->keep,
+                           &c->cells_in, &c->cntl, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->hist, &c->keep,
                            &c->keep_in, &c->uniq, &c->req, &c->found, &c->skey, &c->sval, &c->gflag, &c->gend,
                            &c->gw, &c->lastu, &c->wkeyA, &c->wkeyB, &c->cend, &c->cw, &c->cidxA, &c->cidxB,
                            &c->wsort, &c->means, &c->fra, &c->ops};
