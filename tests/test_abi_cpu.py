@@ -116,3 +116,40 @@ def test_host_checkpoint_resume(tmp_path, lib):
         assert h.setup_rc == 100
     finally:
         os.chdir(cwd)
+
+
+def test_coinc_program_options_without_gpu(tmp_path, lib):
+    """coincidences-gb300 parses the reference's options before touching a
+    device: --help exits 0, a missing -nod fails like handle_opts_coinc
+    (init.c:1112-1116), a missing grid.bin fails with its path."""
+    import subprocess
+    from polgraw_gb300 import build
+    r = subprocess.run([build.COINC_EXE, "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "-mincoin" in r.stdout and "-refloc" in r.stdout
+    r = subprocess.run([build.COINC_EXE, "-data", str(tmp_path)], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "Number of days not set" in r.stdout
+    out = tmp_path / "out"
+    r = subprocess.run([build.COINC_EXE, "-nod", "2", "-output", str(out), "-refloc", str(tmp_path / "nogrid"),
+                        "-snrcutoff", "4.5"], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "grid.bin" in r.stderr
+    assert "corresponding to F-statistic value of 12.125000000000" in r.stdout
+    assert out.is_dir()  # the output directory is created first, as the reference does
+
+
+def test_coinc_create_validates_arguments(lib):
+    from polgraw_gb300.lib import CoincCfg, PA_ERR_ARG, PA_ERR_NODEV
+    cfg = CoincCfg()
+    cfg.N, cfg.mincoin = 86164, 1
+    for j in range(4):
+        cfg.scale[j] = 1
+    st = C.c_int(0)
+    assert not lib.pa_coinc_create(C.byref(cfg), C.byref(st)) and st.value == PA_ERR_ARG
+    assert b"mincoin" in lib.pa_coinc_last_error(None)
+    cfg.mincoin, cfg.scale[2] = 3, 0
+    assert not lib.pa_coinc_create(C.byref(cfg), C.byref(st)) and st.value == PA_ERR_ARG
+    cfg.scale[2] = 1
+    cc = lib.pa_coinc_create(C.byref(cfg), C.byref(st))
+    if lib.pa_device_count() == 0:
+        assert not cc and st.value == PA_ERR_NODEV
+    elif cc:
+        lib.pa_coinc_destroy(cc)
