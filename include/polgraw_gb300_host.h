@@ -77,6 +77,17 @@ const char *pa_host_detector_name(const pa_host *h, int i);
  * process exit code. */
 int pa_coinc_main(int argc, char **argv);
 
+/* Input generation: the reduced Fisher matrix (row-major 4x4) that the grid
+ * generator writes into grid.bin after the grid matrix
+ * (gridgen/src/FisherRM.cpp:17-100, postrmf(xi); ephemeris scaling of
+ * gridgen/src/ReadEphemeris.cpp:82-100), from the ephemeris files' contents:
+ * rSSB and rDet, n x 3 doubles each (Earth w.r.t. the SSB and detector w.r.t.
+ * the Earth's centre), epsm (the obliquity stored at the end of DetSSB.bin)
+ * and the initial time xi (the grid generator's default 0.5).  Equal to the
+ * grid generator's matrix bit for bit.  PA_ERR_ARG for n < 5. */
+int pa_fisher_reduced(const double *rSSB, const double *rDet, long long n, double epsm, double xi,
+                      double *fisher);
+
 #ifdef __cplusplus
 }
 #endif

@@ -161,6 +161,52 @@ def _build_ref_coinc() -> str:
     return REF_COINC
 
 
+REF_GRIDGEN = os.path.join(REF_OUT, "gridgen")
+GRIDGEN_DIR = os.path.join(REFERENCE_ROOT, "gridgen")
+
+
+def _build_ref_gridgen() -> str:
+    """The reference grid generator (gridgen/main.cpp and gridgen/src/*.cpp,
+    C++11 and the standard library only), unmodified, with its own Makefile's
+    language level and no fast-math."""
+    srcs = [os.path.join(GRIDGEN_DIR, "main.cpp")] + sorted(
+        os.path.join(GRIDGEN_DIR, "src", f) for f in os.listdir(os.path.join(GRIDGEN_DIR, "src"))
+        if f.endswith(".cpp"))
+    if not _newer(REF_GRIDGEN, srcs):
+        return REF_GRIDGEN
+    os.makedirs(REF_OUT, exist_ok=True)
+    objdir = os.path.join(REF_OUT, "obj_gridgen")
+    os.makedirs(objdir, exist_ok=True)
+    objs = []
+    for k, src in enumerate(srcs):
+        o = os.path.join(objdir, "%d_%s" % (k, os.path.basename(src).replace(".cpp", ".o")))
+        _run(["g++", "-std=c++11", "-O2", "-ffp-contract=off", "-w", "-I" + os.path.join(GRIDGEN_DIR, "include"),
+              "-c", src, "-o", o])
+        objs.append(o)
+    _run(["g++", "-o", REF_GRIDGEN] + objs)
+    shutil.rmtree(objdir, ignore_errors=True)
+    return REF_GRIDGEN
+
+
+def run_ref_gridgen(ephemeris_dir: str, nfft_exp: int, match: float = 0.75) -> tuple[bytes, str]:
+    """Runs the reference grid generator on a directory holding rSSB.bin,
+    rDet.bin and DetSSB.bin (-m <match> -p dfg -d <dir>/ -n <nfft_exp>).  It
+    reads its covering table dataS2.txt from the working directory, so it
+    runs in a scratch directory holding a copy of the reference's table.
+    Returns (grid.bin bytes, its standard output)."""
+    import tempfile
+    exe = _build_ref_gridgen()
+    with tempfile.TemporaryDirectory() as tmp:
+        shutil.copy(os.path.join(GRIDGEN_DIR, "dataS2.txt"), tmp)
+        r = subprocess.run([exe, "-m", repr(match), "-p", "dfg", "-d", ephemeris_dir.rstrip("/") + "/",
+                            "-n", str(nfft_exp)], cwd=tmp, capture_output=True, text=True,
+                           stdin=subprocess.DEVNULL, timeout=600)
+        if r.returncode != 0:
+            raise RuntimeError("gridgen failed:\n" + r.stdout + r.stderr)
+    with open(os.path.join(ephemeris_dir, "grid.bin"), "rb") as f:
+        return f.read(), r.stdout
+
+
 def build_reference() -> dict:
     """Compile the reference search (serial parity build and OpenMP timing
     build).  Returns {} when the reference checkout is absent."""
@@ -179,6 +225,7 @@ def build_reference() -> dict:
         "src-openmp", REF_OMP, ["-O3", "-ffast-math", "-fopenmp", "-fno-builtin", "-DTIMERS=3"])
     out["followup"] = _build_ref_followup()
     out["coinc"] = _build_ref_coinc()
+    out["gridgen"] = _build_ref_gridgen()
     return out
 
 

@@ -38,6 +38,7 @@ EXPORTS = [
     "pa_coinc_vedva", "pa_coinc_create", "pa_coinc_destroy", "pa_coinc_last_error", "pa_coinc_reset",
     "pa_coinc_add_frame", "pa_coinc_run", "pa_coinc_get", "pa_coinc_cells", "pa_coinc_last_call_ms",
     "pa_coinc_kernel_launches", "pa_coinc_main", "pa_coinc_set_profiling", "pa_coinc_profile_get",
+    "pa_fisher_reduced",
 ]
 
 
@@ -180,6 +181,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.pa_coinc_last_call_ms.argtypes = [C.c_void_p]
     lib.pa_coinc_kernel_launches.restype = C.c_longlong
     lib.pa_coinc_kernel_launches.argtypes = [C.c_void_p]
+    lib.pa_fisher_reduced.argtypes = [P(C.c_double), P(C.c_double), C.c_longlong, C.c_double, C.c_double,
+                                      P(C.c_double)]
     lib.pa_coinc_set_profiling.argtypes = [C.c_void_p, C.c_int]
     lib.pa_coinc_profile_get.argtypes = [C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_longlong)]
     lib.pa_host_create.restype = C.c_void_p
@@ -645,6 +648,18 @@ def read_fisher(grid_path: str) -> np.ndarray:
     """The second 4x4 matrix of grid.bin (manage_grid_matrix, init.c:1155-1167)."""
     raw = open(grid_path, "rb").read()
     return np.frombuffer(raw[4 + 128:4 + 256], dtype="<f8").reshape(4, 4).copy()
+
+
+def fisher_reduced(rssb, rdet, epsm: float, xi: float = 0.5) -> np.ndarray:
+    """pa_fisher_reduced: the grid generator's reduced Fisher matrix from the
+    ephemeris parts (n x 3 each)."""
+    a = np.ascontiguousarray(np.asarray(rssb, dtype=np.float64).reshape(-1))
+    b = np.ascontiguousarray(np.asarray(rdet, dtype=np.float64).reshape(-1))
+    out = np.zeros(16)
+    rc = load().pa_fisher_reduced(_dp(a), _dp(b), len(a) // 3, epsm, xi, _dp(out))
+    if rc != PA_OK:
+        raise SearchError("pa_fisher_reduced failed (%d)" % rc)
+    return out.reshape(4, 4)
 
 
 def vedva(fisher) -> np.ndarray:

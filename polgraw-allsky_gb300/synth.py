@@ -117,11 +117,16 @@ def nsamples(nod: int, dt: float) -> int:
     return int(math.floor(nod * C_SIDDAY / dt + 0.5))
 
 
-def detssb(det: str, N: int, dt: float, gmst0: float = 1.0, orbit0: float = 0.7) -> tuple[np.ndarray, float, float]:
-    """Detector position w.r.t. the SSB in units of c*dt: circular 1 AU orbit
-    in the ecliptic, rotated by the obliquity, plus the site on a spherical
-    Earth rotating at C_OMEGA_R.  Returns (3N array, phir, epsm); phir is the
-    site's local sidereal angle at t=0 (gen2day/ExtractBand.c:336)."""
+def detssb_parts(det: str, N: int, dt: float, gmst0: float = 1.0,
+                 orbit0: float = 0.7) -> tuple[np.ndarray, np.ndarray, float, float]:
+    """The two parts of the detector position in units of c*dt, 3N doubles
+    each (x, y, z interleaved, equatorial): the Earth's centre w.r.t. the SSB
+    (circular 1 AU orbit in the ecliptic, rotated by the obliquity) and the
+    site w.r.t. the Earth's centre (spherical Earth rotating at C_OMEGA_R).
+    The layout of the ephemeris files rSSB.bin and rDet.bin that the grid
+    generator reads (gridgen/src/ReadEphemeris.cpp:24-100).  Returns (rSSB,
+    rDet, phir, epsm); phir is the site's local sidereal angle at t=0
+    (gen2day/ExtractBand.c:336)."""
     site = SITES[det]
     t = np.arange(N, dtype=np.float64) * dt
     unit = C_SPEED_OF_LIGHT * dt                       # km per (c*dt)
@@ -129,21 +134,26 @@ def detssb(det: str, N: int, dt: float, gmst0: float = 1.0, orbit0: float = 0.7)
     so, co = det_sincos(orbit0 + om_orb * t)
     se, ce = det_sincos(np.array([C_EPSMA]))
     r_au = C_AU / unit
-    x = r_au * co
-    y = r_au * so * ce[0]
-    z = r_au * so * se[0]
+    ssb = np.empty(3 * N)
+    ssb[0::3] = r_au * co
+    ssb[1::3] = r_au * so * ce[0]
+    ssb[2::3] = r_au * so * se[0]
     phir = gmst0 + site["elam"]
     sp, cp = det_sincos(phir + C_OMEGA_R * t)
     sphi, cphi = det_sincos(np.array([site["ephi"]]))
     re = C_EARTH_R / unit
-    x = x + re * cphi[0] * cp
-    y = y + re * cphi[0] * sp
-    z = z + re * sphi[0]
-    out = np.empty(3 * N)
-    out[0::3] = x
-    out[1::3] = y
-    out[2::3] = z
-    return out, float(phir), float(C_EPSMA)
+    rdet = np.empty(3 * N)
+    rdet[0::3] = re * cphi[0] * cp
+    rdet[1::3] = re * cphi[0] * sp
+    rdet[2::3] = re * sphi[0]
+    return ssb, rdet, float(phir), float(C_EPSMA)
+
+
+def detssb(det: str, N: int, dt: float, gmst0: float = 1.0, orbit0: float = 0.7) -> tuple[np.ndarray, float, float]:
+    """Detector position w.r.t. the SSB in units of c*dt (rSSB + rDet of
+    detssb_parts).  Returns (3N array, phir, epsm)."""
+    ssb, rdet, phir, epsm = detssb_parts(det, N, dt, gmst0, orbit0)
+    return ssb + rdet, phir, epsm
 
 
 def ast2lin(alfa: float, delta: float, epsm: float = C_EPSMA) -> tuple[list[float], int]:
@@ -226,10 +236,14 @@ def _sha(path: str) -> str:
 def write_dataset(root: str, *, ident: int = 1, band: int = 666, dt: float = 2.0, nod: int = 2,
                   fftpad: int = 1, dets=("H1", "L1"), M: list[float] | None = None,
                   sigma: dict | None = None, seeds: dict | None = None,
-                  gaps: float = 0.0, seed_offset: int = 0) -> Dataset:
+                  gaps: float = 0.0, seed_offset: int = 0, ephemeris_parts: bool = False,
+                  grid_file: str | None = None) -> Dataset:
     """Writes grid.bin, xdatc and DetSSB files.  `gaps` is the fraction of
     samples zeroed in runs (the reference treats exact zeros as gaps:
-    init.c:359-367 and init.c:635)."""
+    init.c:359-367 and init.c:635).  `ephemeris_parts`: also rSSB.bin and
+    rDet.bin per detector (the grid generator's inputs).  `grid_file`: copy
+    this grid.bin (e.g. one made by the grid generator) instead of writing
+    the synthetic one; M is then read from it."""
     N = nsamples(nod, dt)
     ds = Dataset(root=root, ident=ident, band=band, dt=dt, nod=nod, fftpad=fftpad,
                  M=list(M) if M is not None else [], dets=list(dets), N=N)
@@ -238,10 +252,17 @@ def write_dataset(root: str, *, ident: int = 1, band: int = 666, dt: float = 2.0
     base = os.path.join(root, "%03d" % ident)
     os.makedirs(base, exist_ok=True)
     gpath = os.path.join(base, "grid.bin")
-    with open(gpath, "wb") as f:
-        f.write(struct.pack("<i", fftpad))
-        f.write(np.asarray(ds.M, dtype="<f8").tobytes())
-        f.write(np.zeros(32, dtype="<f8").tobytes())
+    if grid_file is not None:
+        raw = open(grid_file, "rb").read()
+        with open(gpath, "wb") as f:
+            f.write(raw)
+        ds.fftpad = struct.unpack("<i", raw[:4])[0]
+        ds.M = list(np.frombuffer(raw[4:132], dtype="<f8"))
+    else:
+        with open(gpath, "wb") as f:
+            f.write(struct.pack("<i", fftpad))
+            f.write(np.asarray(ds.M, dtype="<f8").tobytes())
+            f.write(np.zeros(32, dtype="<f8").tobytes())
     ds.files["grid.bin"] = _sha(gpath)
     sigma = dict(DEFAULT_SIGMA, **(sigma or {}))
     seeds = dict(DEFAULT_SEED, **(seeds or {}))
@@ -260,7 +281,13 @@ def write_dataset(root: str, *, ident: int = 1, band: int = 666, dt: float = 2.0
         xp = os.path.join(dd, "xdatc_%03d_%04d.bin" % (ident, band))
         x.astype("<f8").tofile(xp)
         ds.files[d + "/xdat"] = _sha(xp)
-        pos, phir, epsm = detssb(d, N, dt)
+        ssb, rdet, phir, epsm = detssb_parts(d, N, dt)
+        pos = ssb + rdet
+        if ephemeris_parts:
+            for nm, arr in (("rSSB.bin", ssb), ("rDet.bin", rdet)):
+                ep = os.path.join(dd, nm)
+                arr.astype("<f8").tofile(ep)
+                ds.files[d + "/" + nm[:-4]] = _sha(ep)
         sp_ = os.path.join(dd, "DetSSB.bin")
         with open(sp_, "wb") as f:
             f.write(pos.astype("<f8").tobytes())

@@ -35,9 +35,18 @@ def materialize(case: dict, root: str) -> dict:
     probe = synth.Dataset(root=root, ident=1, band=data["band"], dt=data["dt"], nod=data["nod"],
                           fftpad=data["fftpad"], M=[], dets=list(data["dets"]),
                           N=synth.nsamples(data["nod"], data["dt"]))
-    M = _grid(data, probe)
-    ds = synth.write_dataset(root, ident=1, band=data["band"], dt=data["dt"], nod=data["nod"],
-                             fftpad=data["fftpad"], dets=data["dets"], M=M, gaps=data.get("gaps", 0.0))
+    g = data.get("grid", {})
+    if "gridgen" in g:
+        # a grid.bin made by the reference grid generator from this case's
+        # synthetic ephemeris (make_gridgen_grids.py)
+        ds = synth.write_dataset(root, ident=1, band=data["band"], dt=data["dt"], nod=data["nod"],
+                                 fftpad=data["fftpad"], dets=data["dets"], gaps=data.get("gaps", 0.0),
+                                 ephemeris_parts=True,
+                                 grid_file=os.path.join(os.path.dirname(os.path.abspath(__file__)), g["gridgen"]))
+    else:
+        M = _grid(data, probe)
+        ds = synth.write_dataset(root, ident=1, band=data["band"], dt=data["dt"], nod=data["nod"],
+                                 fftpad=data["fftpad"], dets=data["dets"], M=M, gaps=data.get("gaps", 0.0))
     args = ["-data", root, "-ident", "1", "-band", str(data["band"]), "-dt", repr(data["dt"]),
             "-nod", str(data["nod"])]
     pm = None

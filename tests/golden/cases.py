@@ -15,6 +15,9 @@ Coverage (reference file:line of the behaviour each case exercises):
   h1_fullgrid      no -range/-addsig: gridr sky range (auxi.c:143-212) and the
                    Smin/Smax spindown range with trunc and swap (jobcore.c:424-439)
   h1_nospindown    --nospindown (jobcore.c:444, 456)
+  h1l1_gridgen     a grid made by the reference grid generator (gridgen/) from
+                   the synthetic ephemeris: lower-triangular M with frequency-
+                   sky and frequency-spindown couplings (make_gridgen_grids.py)
   cfg1_h1          the 1-detector N=86164 workload: 1 sky point (delta 0.3,
                    alpha 1.2) x 64 spindowns, injected f=0.1 fdot=-1e-8 SNR 12
 """
@@ -46,6 +49,12 @@ CASES = [
                    grid=dict(m5=-2e-8, sky_scale=0.05)),
          range=[0, 3, -2, 2, -1, 1, 1, 2],
          args=["-threshold", "10", "--nospindown", "--nocheckpoint"]),
+    dict(name="h1l1_gridgen",
+         data=dict(dets=["H1", "L1"], dt=2.0, nod=1, band=666, fftpad=1,
+                   grid=dict(gridgen="grid_h1l1_gridgen.bin", nfft_exp=16)),
+         inject=dict(f=1.3, fdot=0.0, delta=0.5, alpha=2.1, snr=20.0),
+         range=[-2, 2, 0, 1, -4, -3, None, None],
+         args=["-threshold", "16"]),
     dict(name="cfg1_h1",
          data=dict(dets=["H1"], dt=2.0, nod=2, band=666, fftpad=1,
                    grid=dict(m5=-1e-9, sky_point=(0.3, 1.2))),
@@ -83,6 +92,8 @@ FOLLOWUP_CASES = [
 #                     an earlier frame, and a coincidence in the last cell of
 #                     the sorted table (written with multiplicity 0)
 #   coinc_many        24 frames x 5000 records, mincoin 4
+#   coinc_gridgen     the Fisher matrix of a grid made by the reference grid
+#                     generator from the synthetic ephemeris (N=86164)
 COINC_CASES = [
     dict(name="coinc_basic", nod=2, dt=2.0, band=666, frames=[1, 2, 3, 5, 8, 9], per_frame=2000, seed=7,
          refr=3, mincoin=3, shift=0, scale=1111, narrowdown=0.5, snrcutoff=6.0),
@@ -92,4 +103,7 @@ COINC_CASES = [
          refr=2, mincoin=3, shift=0, scale=1111, narrowdown=0.5, snrcutoff=6.0, craft=True),
     dict(name="coinc_many", nod=2, dt=2.0, band=666, frames=list(range(1, 25)), per_frame=5000, seed=3,
          refr=12, mincoin=4, shift=0, scale=1111, narrowdown=0.5, snrcutoff=6.0),
+    dict(name="coinc_gridgen", nod=2, dt=2.0, band=666, frames=[1, 2, 3, 4, 5, 6, 7, 8], per_frame=3000, seed=13,
+         refr=4, mincoin=3, shift=0, scale=1111, narrowdown=0.5, snrcutoff=6.0,
+         grid="grid_coinc_gridgen.bin", nfft_exp=17),
 ]

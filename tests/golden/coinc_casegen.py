@@ -79,11 +79,19 @@ def _oracle_vedva(fis):
     return pyoracle.coinc_vedva(fis)
 
 
+def case_fisher(case: dict, st: dict):
+    from polgraw_gb300 import synth
+    if "grid" in case:
+        raw = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), case["grid"]), "rb").read()
+        return np.frombuffer(raw[4 + 128:4 + 256], dtype="<f8").reshape(4, 4).copy()
+    return synth.fisher_matrix(st["N"], st["oms"])
+
+
 def oracle_cfg(case: dict):
     """pa_coinc_cfg of the case with the oracle's (GSL shim) vedva."""
-    from polgraw_gb300 import lib as L, synth
+    from polgraw_gb300 import lib as L
     st = case_settings(case)
-    fis = synth.fisher_matrix(st["N"], st["oms"])
+    fis = case_fisher(case, st)
     return L.coinc_cfg(N=st["N"], oms=st["oms"], vedva_m=_oracle_vedva(fis), shift=case["shift"],
                        scale=case["scale"], refr=case["refr"], narrowdown=case["narrowdown"],
                        snrcutoff=case["snrcutoff"], mincoin=case["mincoin"])
@@ -97,8 +105,19 @@ def materialize(case: dict, root: str) -> dict:
     st = case_settings(case)
     recs = _records(case, st)
     files = synth.write_triggers(os.path.join(root, "cand"), recs, band=case["band"])
-    fis = synth.fisher_matrix(st["N"], st["oms"])
-    files["grid.bin"] = synth.write_coinc_grid(os.path.join(root, "grid", "grid.bin"), fis)
+    if "grid" in case:
+        # a grid.bin made by the reference grid generator (make_gridgen_grids.py)
+        raw = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), case["grid"]), "rb").read()
+        os.makedirs(os.path.join(root, "grid"), exist_ok=True)
+        gp = os.path.join(root, "grid", "grid.bin")
+        with open(gp, "wb") as f:
+            f.write(raw)
+        fis = np.frombuffer(raw[4 + 128:4 + 256], dtype="<f8").reshape(4, 4).copy()
+        import hashlib
+        files["grid.bin"] = hashlib.sha256(raw).hexdigest()
+    else:
+        fis = synth.fisher_matrix(st["N"], st["oms"])
+        files["grid.bin"] = synth.write_coinc_grid(os.path.join(root, "grid", "grid.bin"), fis)
     os.makedirs(os.path.join(root, "out"), exist_ok=True)
     args = ["-data", os.path.join(root, "cand"), "-output", os.path.join(root, "out"),
             "-refr", str(case["refr"]), "-fpo", repr(st["fpo"]), "-dt", repr(case["dt"]),

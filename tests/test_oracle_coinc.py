@@ -8,6 +8,7 @@ the oracle's."""
 import base64
 import hashlib
 import platform
+import struct
 
 import numpy as np
 import pytest
@@ -83,3 +84,31 @@ def test_digits_and_cfg():
     c = L.coinc_cfg(N=10, oms=1.0, vedva_m=np.eye(4), shift=1011, scale=2402, narrowdown=0.25)
     assert list(c.shift) == [1, 0, 1, 1] and list(c.scale) == [2, 4, 1, 2]
     assert c.narrowdown == 0.25 * np.pi
+
+
+def test_fisher_reduced_matches_grid_generator(lib):
+    """pa_fisher_reduced from the synthetic ephemeris parts equals, bit for
+    bit, the reduced Fisher matrix that the reference grid generator wrote
+    into each committed grid fixture (make_gridgen_grids.py)."""
+    import json
+    import os
+    import tempfile
+    from polgraw_gb300 import lib as L, synth
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    rec = json.load(open(os.path.join(here, "gridgen_grids.json")))
+    assert rec
+    for name, r in rec.items():
+        sp = r["spec"]
+        raw = open(os.path.join(here, name), "rb").read()
+        assert hashlib.sha256(raw).hexdigest() == r["sha256"]
+        N = synth.nsamples(sp["nod"], sp["dt"])
+        ssb, rdet, phir, epsm = synth.detssb_parts(sp["det"], N, sp["dt"])
+        with tempfile.TemporaryDirectory() as tmp:
+            ds = synth.write_dataset(tmp, ident=1, band=sp["band"], dt=sp["dt"], nod=sp["nod"], dets=[sp["det"]],
+                                     ephemeris_parts=True)
+            assert {k: v for k, v in ds.files.items() if "/" in k} == r["ephemeris"]
+        F = L.fisher_reduced(ssb, rdet, epsm)
+        G = np.frombuffer(raw[4 + 128:4 + 256], dtype="<f8").reshape(4, 4)
+        assert np.array_equal(F, G), (name, F - G)
+        # and the grid's fftpad is the one the search derives for this length
+        assert struct.unpack("<i", raw[:4])[0] == sp["nfft_exp"] - int(np.ceil(np.log2(N))) + 1
