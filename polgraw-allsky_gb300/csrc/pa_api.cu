@@ -56,13 +56,22 @@ struct pa_ctx {
   pa::Prof prof;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.;
-  // CUDA graph of a batch (captured launches, updated in place when the next
-  // batch has the same launch structure)
+  // CUDA graphs of a batch, one per part of the batch (captured launches,
+  // updated in place when the next batch has the same launch structure)
   bool graphs = false;
-  cudaGraphExec_t gexec = nullptr;
+  std::vector<cudaGraphExec_t> gexec_parts;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int sb_max = 0;  // spindown batch the buffers are sized for
 };
+
+// sky points per captured part of a batch (launch_tasks)
+constexpr size_t kGraphPart = 256;
+
+static void drop_graphs(pa_ctx* c) {
+  for (auto& g : c->gexec_parts)
+    if (g) cudaGraphExecDestroy(g);
+  c->gexec_parts.clear();
+}
 
 namespace pa {
 const char* kernel_kind_name(int k) {
@@ -422,7 +431,7 @@ void pa_destroy(pa_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
-  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  drop_graphs(c);
   for (void* p : c->allocs) cudaFree(p);
   if (c->h_cand) cudaFreeHost(c->h_cand);
   if (c->h_ncand) cudaFreeHost(c->h_ncand);
@@ -633,19 +642,21 @@ bool cand_less(const pa::DevCand& x, const pa::DevCand& y) {
   return x.ii < y.ii;
 }
 
-// Enqueues a batch on the context's streams: the candidate counter reset,
-// then every sky point (prelude on the prelude stream forked from the main
-// stream, spindowns on the main stream), and the join of the prelude stream
-// back into the main stream.  Slots are reused across sky points through
-// their events; the first use of each slot in a batch needs no wait (the
-// previous batch finished before this call).  Works unchanged under stream
-// capture.
-int enqueue_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
-  CK(cudaMemsetAsync(c->b.ncand, 0, sizeof(int), c->stream), "memset");
+// Enqueues sky points [t0, t1) of a batch on the context's streams: the
+// candidate counter reset (for the batch's first part), then every sky point
+// (prelude on the prelude stream forked from the main stream, spindowns on
+// the main stream), and the join of the prelude stream back into the main
+// stream.  Slots are reused across sky points through their events; the
+// first use of each slot in a part needs no wait (the work before it on the
+// main stream -- the previous part or call -- has finished when the part
+// starts).  Works unchanged under stream capture.
+int enqueue_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o, size_t t0, size_t t1,
+                  bool reset) {
+  if (reset) CK(cudaMemsetAsync(c->b.ncand, 0, sizeof(int), c->stream), "memset");
   CK(cudaEventRecord(c->ev_fork, c->stream), "cudaEventRecord");
   CK(cudaStreamWaitEvent(c->stream_pre, c->ev_fork, 0), "cudaStreamWaitEvent");
   bool used[2] = {false, false};
-  for (size_t t = 0; t < hs.size(); t++) {
+  for (size_t t = t0; t < t1; t++) {
     if (!hs[t].inside || hs[t].nss == 0) continue;
     const int slot = (int)t & 1;
     int rc = enqueue_sky(c, hs[t], o, (int)t, nullptr, 0, used[slot]);
@@ -655,6 +666,10 @@ int enqueue_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
   CK(cudaEventRecord(c->ev_join, c->stream_pre), "cudaEventRecord");
   CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "cudaStreamWaitEvent");
   return PA_OK;
+}
+
+int enqueue_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
+  return enqueue_tasks(c, hs, o, 0, hs.size(), true);
 }
 
 // Replaces *exec by an executable graph of g: updated in place when the
@@ -685,20 +700,32 @@ int launch_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
     CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
     return enqueue_tasks(c, hs, o);
   }
-  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-  int rc = enqueue_tasks(c, hs, o);
-  cudaGraph_t g = nullptr;
-  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-  if (rc) {
-    if (g) cudaGraphDestroy(g);
-    return rc;
+  // The batch is captured in parts of about kGraphPart sky points, each into
+  // its own executable graph (updated in place when the part's launch
+  // structure repeats), and each part is launched as soon as it is captured:
+  // the host captures part k + 1 while the device runs part k, so only the
+  // first part's capture precedes device work.
+  const size_t n = hs.size();
+  const size_t nparts = std::max<size_t>(1, (n + kGraphPart - 1) / kGraphPart);
+  const size_t per = (n + nparts - 1) / nparts;
+  if (c->gexec_parts.size() < nparts) c->gexec_parts.resize(nparts, nullptr);
+  for (size_t k = 0; k < nparts; k++) {
+    const size_t t0 = k * per, t1 = std::min(n, t0 + per);
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    int rc = enqueue_tasks(c, hs, o, t0, t1, k == 0);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+    rc = graph_exec_from(g, &c->gexec_parts[k], &c->err);
+    cudaGraphDestroy(g);
+    if (rc) return rc;
+    if (k == 0) CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
+    CK(cudaGraphLaunch(c->gexec_parts[k], c->stream), "cudaGraphLaunch");
   }
-  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
-  rc = graph_exec_from(g, &c->gexec, &c->err);
-  cudaGraphDestroy(g);
-  if (rc) return rc;
-  CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
-  CK(cudaGraphLaunch(c->gexec, c->stream), "cudaGraphLaunch");
   return PA_OK;
 }
 
@@ -740,10 +767,7 @@ int grow_candidates(pa_ctx* c, int n) {
   c->eng->prof = &c->prof;
   c->eng->set_split(split);
   c->extra_launches += before;
-  if (c->gexec) {
-    cudaGraphExecDestroy(c->gexec);
-    c->gexec = nullptr;
-  }
+  drop_graphs(c);
   return PA_OK;
 }
 
@@ -853,10 +877,9 @@ int pa_search_batch(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o
 int pa_set_graphs(pa_ctx* c, int on) {
   if (!c) return PA_ERR_ARG;
   c->graphs = on != 0;
-  if (!c->graphs && c->gexec) {
+  if (!c->graphs && !c->gexec_parts.empty()) {
     cudaSetDevice(c->dev);
-    cudaGraphExecDestroy(c->gexec);
-    c->gexec = nullptr;
+    drop_graphs(c);
   }
   return PA_OK;
 }
@@ -915,10 +938,7 @@ int pa_autotune(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o, co
   }
   c->b.sbatch = bsb;
   c->eng->set_split(bsp);
-  if (c->gexec) {
-    cudaGraphExecDestroy(c->gexec);
-    c->gexec = nullptr;
-  }
+  drop_graphs(c);
   if (sbatch) *sbatch = bsb;
   if (split) *split = bsp;
   return PA_OK;
