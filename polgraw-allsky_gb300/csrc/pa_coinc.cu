@@ -865,6 +865,7 @@ struct pa_coinc {
   size_t h_recs_cap = 0, h_mem_cap = 0;
   long long n_in = 0;
   const unsigned* val_sorted = nullptr;  // in-band index of each sorted position (last run)
+  bool ev1_done = false;                 // the run's end event is already on the stream
 };
 
 static std::string g_coinc_create_error;
@@ -1404,6 +1405,9 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
       CCK(cudaMemcpyAsync(c->h_fra, c->fra.p, sizeof(int) * M, cudaMemcpyDeviceToHost, c->stream), "copy");
       CCK(cudaMemcpyAsync(c->h_ops, c->ops.p, sizeof(int) * M, cudaMemcpyDeviceToHost, c->stream), "copy");
     }
+    // the device work ends here; what follows is host bookkeeping
+    CCK(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
+    c->ev1_done = true;
     CCK(cudaStreamSynchronize(c->stream), "sync");
     c->sum.nmembers = M;
   }
@@ -1445,6 +1449,7 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
   c->sum.raw = c->nraw;
   c->n_in = 0;
   c->val_sorted = nullptr;
+  c->ev1_done = false;
   CCK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
   // frame table
   memset(&c->ft, 0, sizeof(c->ft));
@@ -1562,7 +1567,7 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
       if (rc) return rc;
     }
   }
-  CCK(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
+  if (!c->ev1_done) CCK(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
   CCK(cudaEventSynchronize(c->ev1), "cudaEventSynchronize");
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);

@@ -777,13 +777,14 @@ class Coinc:
         s = CoincSummary()
         self._check(self.lib.pa_coinc_run(self.cc, C.byref(s)), "pa_coinc_run")
         fi = np.zeros((max(1, s.nframes), 3), dtype=np.int32)
-        recs = (CoincRec * max(1, s.ncoin))()
-        fra = np.zeros(max(1, s.nmembers), dtype=np.int32)
-        ops = np.zeros(max(1, s.nmembers), dtype=np.int32)
+        recs = np.empty(max(1, s.ncoin), dtype=COINC_REC_DTYPE)
+        fra = np.empty(max(1, s.nmembers), dtype=np.int32)
+        ops = np.empty(max(1, s.nmembers), dtype=np.int32)
         IP = C.POINTER(C.c_int)
-        self._check(self.lib.pa_coinc_get(self.cc, fi.ctypes.data_as(IP), recs, fra.ctypes.data_as(IP),
-                                          ops.ctypes.data_as(IP)), "pa_coinc_get")
-        w, first, mean = coinc_recs(recs, s.ncoin)
+        self._check(self.lib.pa_coinc_get(self.cc, fi.ctypes.data_as(IP), recs.ctypes.data_as(C.POINTER(CoincRec)),
+                                          fra.ctypes.data_as(IP), ops.ctypes.data_as(IP)), "pa_coinc_get")
+        recs = recs[:s.ncoin]
+        w, first, mean = recs["w"], recs["first"], recs["mean"]
         cl = kp = None
         if cells:
             cl = np.zeros((max(1, s.inband), 4), dtype=np.int32)
