@@ -257,7 +257,7 @@ __device__ __forceinline__ unsigned block_flag_prefix(int flag, unsigned* sh, un
 __global__ void __launch_bounds__(kT) k_cells(const double* __restrict__ rec, CellArgs a,
                                               int4* __restrict__ cells_raw, uint8_t* __restrict__ flag,
                                               unsigned* __restrict__ blk_cnt, int* __restrict__ minmax,
-                                              unsigned* __restrict__ nexact) {
+                                              unsigned* __restrict__ nexact, double* __restrict__ snr_raw) {
   __shared__ unsigned sh[kT / 32];
   __shared__ int smm[8];
   const int b = blockIdx.x;
@@ -277,6 +277,7 @@ __global__ void __launch_bounds__(kT) k_cells(const double* __restrict__ rec, Ce
     const int ok = cell_of(rec + 5 * r, fshift, a, &cl, nexact);
     flag[r] = (uint8_t)ok;
     cells_raw[r] = cl;
+    snr_raw[r] = rec[5 * r + 4];
     if (ok) {
       cnt++;
       mn[0] = min(mn[0], cl.x); mx[0] = max(mx[0], cl.x);
@@ -352,7 +353,8 @@ template <typename K>
 __global__ void __launch_bounds__(kT) k_inband(const uint8_t* __restrict__ flag, const int4* __restrict__ cells_raw,
                                                const unsigned* __restrict__ blk_off, KeyLayout L,
                                                unsigned* __restrict__ rawidx, int4* __restrict__ cells_in,
-                                               K* __restrict__ key, unsigned* __restrict__ val) {
+                                               K* __restrict__ key, unsigned* __restrict__ val,
+                                               const double* __restrict__ snr_raw, double* __restrict__ snr_in) {
   __shared__ unsigned sh[kT / 32];
   const int b = blockIdx.x;
   const int f = frame_of_block(b);
@@ -372,6 +374,7 @@ __global__ void __launch_bounds__(kT) k_inband(const uint8_t* __restrict__ flag,
       cells_in[o] = cl;
       key[o] = make_key<K>(cl, L);
       val[o] = o;
+      snr_in[o] = snr_raw[r];
     }
     base += tot;
   }
@@ -631,8 +634,8 @@ __global__ void k_frame_find(const int2* __restrict__ req, int nreq, const unsig
 
 template <typename K>
 __global__ void __launch_bounds__(kT) k_dedup(const K* __restrict__ key, const unsigned* __restrict__ val,
-                                              const unsigned* __restrict__ rawidx, const double* __restrict__ rec,
-                                              long long n, uint8_t* __restrict__ keep, unsigned* __restrict__ uniq) {
+                                              const double* __restrict__ snr_in, long long n,
+                                              uint8_t* __restrict__ keep, unsigned* __restrict__ uniq) {
   __shared__ unsigned hcount[256];
   __shared__ unsigned s_in[kMaxFrames + 1];
   hcount[threadIdx.x] = 0;
@@ -643,8 +646,8 @@ __global__ void __launch_bounds__(kT) k_dedup(const K* __restrict__ key, const u
     const K k0 = key[i];
     const unsigned v0 = val[i];
     const int f = frame_of_in(v0, s_in, nf);
-    bool start = (i == 0);
-    if (!start) start = !(key[i - 1] == k0) || frame_of_in(val[i - 1], s_in, nf) != f;
+    // the previous record's frame matters only when its cells are equal
+    const bool start = (i == 0) || !(key[i - 1] == k0) || frame_of_in(val[i - 1], s_in, nf) != f;
     uint8_t kept = 0;
     if (start) {
       const long long fs = s_in[f];
@@ -654,10 +657,12 @@ __global__ void __launch_bounds__(kT) k_dedup(const K* __restrict__ key, const u
       // coincidences.c:317-413 over the pairs (t, t + 1) of the run
       long long maxsnridx = 0, maxi = i;
       double candsnr = 0;
+      unsigned vt = v0;
+      double s0 = j > i ? snr_in[vt] : 0.;
       for (long long t = i; t < j; t++) {
-        const long long idx = (long long)val[t] - fs, idx1 = (long long)val[t + 1] - fs;
-        const double s0 = rec[5 * (long long)rawidx[val[t]] + 4];
-        const double s1 = rec[5 * (long long)rawidx[val[t + 1]] + 4];
+        const unsigned vt1 = val[t + 1];
+        const double s1 = snr_in[vt1];
+        const long long idx = (long long)vt - fs, idx1 = (long long)vt1 - fs;
         if (!maxsnridx) {
           maxsnridx = (s0 > s1) ? idx : idx1;
           maxi = (s0 > s1) ? t : t + 1;
@@ -669,6 +674,8 @@ __global__ void __launch_bounds__(kT) k_dedup(const K* __restrict__ key, const u
             maxsnridx = idx1; maxi = t + 1; candsnr = s1;
           }
         }
+        vt = vt1;
+        s0 = s1;
       }
       const bool dropped = c_ft.drop[f] && key_is(k0, c_ft.drop_lo[f], c_ft.drop_hi[f]);
       if (!dropped) {
@@ -843,7 +850,7 @@ struct pa_coinc {
     void* p = nullptr;
     size_t n = 0;
   };
-  Buf rec, cells_raw, flag, blkcnt, scan_tmp, minmax, rawidx, cells_in, cntl, keyA, keyB, valA, valB, hist,
+  Buf rec, cells_raw, flag, snr_raw, blkcnt, scan_tmp, minmax, rawidx, cells_in, snr_in, cntl, keyA, keyB, valA, valB, hist,
       keep, keep_in, uniq, req, found, skey, sval, gflag, gend, gw, lastu, wkeyA, wkeyB, cend, cw, cidxA, cidxB,
       wsort, means, fra, ops;
   // optional per-kernel profile: events around each launch while on
@@ -1097,8 +1104,8 @@ void pa_coinc_destroy(pa_coinc* c) {
   if (!c) return;
   cudaSetDevice(c->cfg.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  pa_coinc::Buf* bufs[] = {&c->rec, &c->cells_raw, &c->flag, &c->blkcnt, &c->scan_tmp, &c->minmax, &c->rawidx,
-                           &c->cells_in, &c->cntl, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->hist, &c->keep,
+  pa_coinc::Buf* bufs[] = {&c->rec, &c->cells_raw, &c->flag, &c->snr_raw, &c->blkcnt, &c->scan_tmp, &c->minmax, &c->rawidx,
+                           &c->cells_in, &c->snr_in, &c->cntl, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->hist, &c->keep,
                            &c->keep_in, &c->uniq, &c->req, &c->found, &c->skey, &c->sval, &c->gflag, &c->gend,
                            &c->gw, &c->lastu, &c->wkeyA, &c->wkeyB, &c->cend, &c->cw, &c->cidxA, &c->cidxB,
                            &c->wsort, &c->means, &c->fra, &c->ops};
@@ -1170,6 +1177,7 @@ template <typename K>
 static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<long long>& nin_f) {
   const int nf = (int)c->frames.size();
   const long long n = c->n_in;
+  ENS(snr_in, sizeof(double) * n);
   ENS(keyA, sizeof(K) * n);
   ENS(keyB, sizeof(K) * n);
   ENS(valA, sizeof(unsigned) * n);
@@ -1178,7 +1186,8 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
     Span sp_(c, CK_INBAND);
     k_inband<K><<<nblk1, kT, 0, c->stream>>>(P<uint8_t>(c->flag), P<int4>(c->cells_raw), P<unsigned>(c->blkcnt), L,
                                              P<unsigned>(c->rawidx), P<int4>(c->cells_in),
-                                             P<K>(c->keyA), P<unsigned>(c->valA));
+                                             P<K>(c->keyA), P<unsigned>(c->valA), P<double>(c->snr_raw),
+                                             P<double>(c->snr_in));
   }
   c->launches++;
   CCK(cudaGetLastError(), "k_inband");
@@ -1267,9 +1276,8 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
   c->val_sorted = val;
   {
     Span sp_(c, CK_DEDUP);
-    k_dedup<K><<<(unsigned)((n + kT - 1) / kT), kT, 0, c->stream>>>(key, val, P<unsigned>(c->rawidx),
-                                                                    P<double>(c->rec), n, P<uint8_t>(c->keep),
-                                                                    P<unsigned>(c->uniq));
+    k_dedup<K><<<(unsigned)((n + kT - 1) / kT), kT, 0, c->stream>>>(key, val, P<double>(c->snr_in), n,
+                                                                    P<uint8_t>(c->keep), P<unsigned>(c->uniq));
   }
   c->launches++;
   CCK(cudaGetLastError(), "k_dedup");
@@ -1505,6 +1513,7 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
     }
     ENS(cells_raw, sizeof(int4) * c->nraw);
     ENS(flag, c->nraw);
+    ENS(snr_raw, sizeof(double) * c->nraw);
     ENS(blkcnt, sizeof(unsigned) * (nblk1 + 1));
     ENS(scan_tmp, sizeof(unsigned) * scan_tmp_len(nblk1 + 1));
     ENS(minmax, sizeof(int) * 9);
@@ -1514,7 +1523,7 @@ int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
       Span sp_(c, CK_CELLS);
       k_cells<<<nblk1, kT, 0, c->stream>>>(P<double>(c->rec), a, P<int4>(c->cells_raw), P<uint8_t>(c->flag),
                                           P<unsigned>(c->blkcnt), P<int>(c->minmax),
-                                          (unsigned*)(P<int>(c->minmax) + 8));
+                                          (unsigned*)(P<int>(c->minmax) + 8), P<double>(c->snr_raw));
     }
     c->launches++;
     CCK(cudaGetLastError(), "k_cells");
