@@ -2,7 +2,8 @@
 reference grid generator (gridgen/, compiled from its own sources by
 oracle/build_oracle.py into oracle/_ref/gridgen) from the synthetic
 ephemeris of each case that names one (cases.py: a search case with
-data.grid.gridgen, a coincidence case with "grid"): rSSB.bin, rDet.bin and
+data.grid.gridgen, a coincidence case with "grid"; the pipeline case's Fisher
+matrix, pipeline_case.py): rSSB.bin, rDet.bin and
 DetSSB.bin of the case's first detector (polgraw_gb300.synth.detssb_parts),
 `gridgen -m 0.75 -p dfg -d <dir>/ -n <log2 nfft>`.  The ephemeris files are
 regenerated bit for bit from the case parameters, so only the 388-byte grids
@@ -57,6 +58,9 @@ def gridgen_specs() -> list[dict]:
         if "grid" in c:
             out.append(dict(file=c["grid"], det="H1", dt=c["dt"], nod=c["nod"], band=c["band"],
                             nfft_exp=c["nfft_exp"]))
+    from pipeline_case import PIPELINE as P
+    out.append(dict(file=P["fisher_grid"], det=P["dets"][0], dt=P["dt"], nod=P["nod"], band=P["band"],
+                    nfft_exp=P["nfft_exp"]))
     return out
 
 

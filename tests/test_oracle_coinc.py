@@ -7,6 +7,7 @@ Also the library's host-side transformation matrix (pa_coinc_vedva) against
 the oracle's."""
 import base64
 import hashlib
+import os
 import platform
 import struct
 
@@ -15,7 +16,7 @@ import pytest
 
 from cases import COINC_CASES
 from coinc_casegen import materialize, oracle_cfg
-from helpers import canon_coi, golden, parse_coi
+from helpers import GOLDEN_DIR, canon_coi, golden, parse_coi
 
 
 @pytest.fixture(scope="module", params=[c["name"] for c in COINC_CASES])
@@ -112,3 +113,30 @@ def test_fisher_reduced_matches_grid_generator(lib):
         assert np.array_equal(F, G), (name, F - G)
         # and the grid's fftpad is the one the search derives for this length
         assert struct.unpack("<i", raw[:4])[0] == sp["nfft_exp"] - int(np.ceil(np.log2(N))) + 1
+
+
+def test_oracle_on_reference_pipeline_triggers():
+    """The coincidence oracle over the trigger files the reference search
+    wrote for the pipeline case (tests/golden/pipeline_h1l1.json), in the
+    order the reference coincidence program read them, reproduces that
+    program's .coi file and summary line."""
+    import re
+    import pyoracle
+    from pipeline_case import PIPELINE, settings
+    from polgraw_gb300 import lib as L
+    g = golden("pipeline_h1l1")
+    st = settings(PIPELINE)
+    raw = open(os.path.join(GOLDEN_DIR, PIPELINE["fisher_grid"]), "rb").read()
+    fis = np.frombuffer(raw[132:260], dtype="<f8").reshape(4, 4)
+    cfg = L.coinc_cfg(N=st["N"], oms=st["oms"], vedva_m=pyoracle.coinc_vedva(fis), refr=PIPELINE["refr"],
+                      mincoin=PIPELINE["mincoin"], snrcutoff=PIPELINE["snrcutoff"],
+                      narrowdown=PIPELINE["narrowdown"])
+    by_frame = {int(re.match(r"triggers_(\d+)_", n).group(1)): np.array(r).reshape(-1, 5)
+                for n, r in g["trigger_files"].items()}
+    res = pyoracle.coinc(cfg, g["order"], [by_frame[f] for f in g["order"]])
+    assert res.frameinfo.tolist() == g["frameinfo"]
+    coi = base64.b64decode(g["coi_b64"])
+    assert canon_coi(res.coi_bytes()) == canon_coi(coi)
+    assert res.summary_line("%04d" % PIPELINE["band"], 0, st["fpo"]) == g["stderr"]
+    # the injection is found in every segment
+    assert res.summary.maxcoin == len(PIPELINE["frames"])
