@@ -438,7 +438,7 @@ int pa_coinc_get(const pa_coinc *cc, int *frameinfo, pa_coinc_rec *recs, int *fr
  * order (frame by frame), cells[inband][4] (fi, si, di, ai of
  * coincidences.c:256-261) and keep[inband] = 1 for the record each
  * frame's duplicate removal keeps. */
-int pa_coinc_cells(const pa_coinc *cc, int *cells, unsigned char *keep);
+int pa_coinc_cells(pa_coinc *cc, int *cells, unsigned char *keep);
 double pa_coinc_last_call_ms(const pa_coinc *cc);
 long long pa_coinc_kernel_launches(const pa_coinc *cc);
 /* Per-kernel profile of the following runs (CUDA events around every

@@ -1595,8 +1595,7 @@ int pa_coinc_get(const pa_coinc* c, int* frameinfo, pa_coinc_rec* recs, int* fra
   return PA_OK;
 }
 
-int pa_coinc_cells(const pa_coinc* cc, int* cells, unsigned char* keep) {
-  pa_coinc* c = const_cast<pa_coinc*>(cc);
+int pa_coinc_cells(pa_coinc* c, int* cells, unsigned char* keep) {
   if (!c) return PA_ERR_ARG;
   if (c->n_in <= 0) return PA_OK;
   CCK(cudaSetDevice(c->cfg.device), "cudaSetDevice");
