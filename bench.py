@@ -510,6 +510,30 @@ def run_coinc(args, L):
     emit(line)
 
 
+def coinc_extra(L, steps: int = 3) -> dict:
+    """The coincidence step (trigger-file consumer) on a smaller workload than
+    --workload coincidences: 24 frames x 2^18 records, device time per run."""
+    w = workloads.coincidences(24, 1 << 18)
+    cfg = L.coinc_cfg(N=w["N"], oms=w["oms"], vedva_m=L.vedva(w["fisher"]), refr=w["refr"], mincoin=w["mincoin"])
+    cc = L.Coinc(cfg)
+    for f in w["frames"]:
+        cc.add_frame(f, w["recs"][f])
+    for _ in range(2):
+        cc.run()
+    ms = 0.0
+    for _ in range(steps):
+        l2_flush()
+        res = cc.run()
+        ms += cc.last_call_ms()
+    cc.close()
+    nrec = int(res.summary.raw)
+    return {"metric": "trigger records/s through the coincidence step", "value": nrec * steps / (ms / 1e3),
+            "unit": "records/s", "ms_per_run": ms / steps, "records": nrec,
+            "coincidences": int(res.summary.ncoin),
+            "workload": "24 frames x 262144 trigger records, N=86164, 64 lines x 256 sky, 1000 signals, mincoin 4 "
+                        "(bench.py --workload coincidences: 24 x 2^20)"}
+
+
 _JSON_FD = 1
 
 
@@ -748,6 +772,8 @@ def main():
                                                          default=0.0),
                                 "index_mismatches": sum(1 for k in ref if k not in got and not edge(ref[k])) +
                                 sum(1 for k in got if k not in ref and not edge(got[k]))}
+    if not args.no_extras and rank == 0:
+        out["coincidences"] = coinc_extra(L)
     if rank == 0:
         emit(out)
     ctx.close()
