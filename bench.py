@@ -534,6 +534,36 @@ def coinc_extra(L, steps: int = 3) -> dict:
                         "(bench.py --workload coincidences: 24 x 2^20)"}
 
 
+def followup_extra(L, steps: int = 3) -> dict:
+    """The followup F-statistic (demodulated, BASELINE config 5 shape: H1+L1+V1,
+    N=86164, 4096 candidates) and its adjoint gradient, device time per batch
+    in the default mixed form (FP64 phase) and with the two-float phase."""
+    tmp = tempfile.mkdtemp(prefix="pa_followup_")
+    argv, inj = workloads.followup(tmp)
+    host = L.Host(argv)
+    dets, nifo = host.detectors()
+    pts, ws, which = workloads.candidates_around(host, inj, 4096)
+    out = {"metric": "demodulated F-statistic evaluations/s (followup)", "unit": "evals/s", "candidates": len(pts),
+           "workload": "H1+L1+V1, N=86164 dt=2s, 4096 candidates around 4 injections "
+                       "(bench.py --workload followup has the ascent, the simplex and the CPU baseline)"}
+    for name, ph in (("mixed", L.PA_PHASE_F64), ("mixed_ffphase", L.PA_PHASE_FF)):
+        fu = L.Followup(host.settings, dets, nifo, precision=L.PA_PREC_MIXED, phase_mode=ph)
+        fu.fstatnet(pts)
+        fu.fstatnet_grad(pts)
+        ms = gms = 0.0
+        for _ in range(steps):
+            l2_flush()
+            fu.fstatnet(pts)
+            ms += fu.last_call_ms()
+            l2_flush()
+            fu.fstatnet_grad(pts)
+            gms += fu.last_call_ms()
+        out[name] = {"fstat_evals_per_s": len(pts) * steps / (ms / 1e3),
+                     "grad_evals_per_s": len(pts) * steps / (gms / 1e3)}
+        fu.close()
+    return out
+
+
 _JSON_FD = 1
 
 
@@ -774,6 +804,7 @@ def main():
                                 sum(1 for k in got if k not in ref and not edge(got[k]))}
     if not args.no_extras and rank == 0:
         out["coincidences"] = coinc_extra(L)
+        out["followup"] = followup_extra(L)
     if rank == 0:
         emit(out)
     ctx.close()
