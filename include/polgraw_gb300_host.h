@@ -35,7 +35,8 @@ typedef struct pa_host pa_host;
 enum {
   PA_HOST_OK = 0,
   PA_HOST_EXIT_SUCCESS = 100,  /* reference would exit(EXIT_SUCCESS) here */
-  PA_HOST_EXIT_FAILURE = 101   /* reference would exit(EXIT_FAILURE) here */
+  PA_HOST_EXIT_FAILURE = 101,  /* reference would exit(EXIT_FAILURE) here */
+  PA_HOST_INTERRUPTED = 102    /* stopped by PA_HOST_STOP_AT_SKY (pa_host_search) */
 };
 
 /* handle_opts(): parses argv (getopt_long_only, same option table) plus the
@@ -54,7 +55,11 @@ int pa_host_setup(pa_host *h);
 /* search() (jobcore.c:51-184) over the context: state file before each
  * sky point, locked append of the candidate buffer when it holds more than
  * nfft records and at the end of each hemisphere, state file emptied at the
- * end (main.c:142-147).  Returns PA_HOST_OK or PA_HOST_EXIT_FAILURE. */
+ * end (main.c:142-147).  Returns PA_HOST_OK or PA_HOST_EXIT_FAILURE.
+ * Fault injection: with the environment variable PA_HOST_STOP_AT_SKY=k it
+ * stops like a crash after writing the state file of its k-th sky-point
+ * batch (0-based): buffered candidates are dropped, the state file stays,
+ * and it returns PA_HOST_INTERRUPTED (the program exits with status 3). */
 int pa_host_search(pa_host *h, pa_ctx *ctx);
 
 /* Runs the whole program (gwsearch-gb300 main). */

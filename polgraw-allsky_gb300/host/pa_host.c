@@ -1020,6 +1020,13 @@ int pa_host_search(pa_host *h, pa_ctx *ctx) {
   const int skyb = h->opts.skybatch > 0 ? h->opts.skybatch : 1;
   pa_sky *tasks = (pa_sky *)malloc(sizeof(pa_sky) * skyb);
   int rc_out = PA_HOST_OK;
+  /* Host-side fault injection (tests of checkpoint/resume): with
+   * PA_HOST_STOP_AT_SKY=k the search stops like a crash right after writing
+   * the state file for its k-th sky-point batch (0-based), before that
+   * batch's GPU work: buffered candidates are dropped, the state file stays. */
+  const char *stop_env = getenv("PA_HOST_STOP_AT_SKY");
+  const long stop_at = stop_env ? strtol(stop_env, NULL, 10) : -1;
+  long batch_no = 0;
 
   for (int pm = r->pst; pm <= r->pmr[1]; ++pm) {
     snprintf(outname, sizeof outname, "%s/triggers_%03d_%04d%s_%d.bin", h->opts.prefix,
@@ -1042,6 +1049,10 @@ int pa_host_search(pa_host *h, pa_ctx *ctx) {
         if (ftruncate(fileno(state), 0)) perror("ftruncate");
         fprintf(state, "%d %d %d %d %d\n", pm, tasks[0].mm, tasks[0].nn, r->sst, h->FNum);
         fseek(state, 0, SEEK_SET);
+      }
+      if (batch_no++ == stop_at) {
+        rc_out = PA_HOST_INTERRUPTED;
+        goto done;
       }
       for (;;) {
         int needed = 0, st;
@@ -1122,6 +1133,7 @@ int pa_host_main(int argc, char **argv) {
     if (state) fclose(state);
   }
   pa_host_destroy(h);
+  if (rc == PA_HOST_INTERRUPTED) return 3;
   return rc == PA_HOST_OK ? 0 : 1;
 }
 

@@ -5,13 +5,17 @@
 * the device candidate buffer (2^18 candidates) overflowing: the context
   grows it and re-runs the batch, with the same records as a later run;
 * an empty batch and sky points outside the grid disk (jobcore.c:248): no
-  records, FNum unchanged.
+  records, FNum unchanged;
+* a crash between sky points (host-side fault injection) and the restart
+  from the state file.
 """
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
 
+from casegen import materialize
 from helpers import case_by_name, key_of, make_host
 
 pytestmark = pytest.mark.gpu
@@ -76,3 +80,46 @@ def test_empty_batch_and_outside_disk(tmp_path, gpu_ok):
     far = int(3 * s.oms / max(abs(s.M[10]), abs(s.M[15]))) + 1
     rec, idx, fnum = ctx.job_core(1, far, far, host.opts(), host.range)
     assert len(rec) == 0 and fnum == 0
+
+
+def test_crash_and_resume(tmp_path, gpu_ok):
+    """Host-side fault injection: gwsearch-gb300 stopped like a crash after
+    writing the state file of its 4th sky point (PA_HOST_STOP_AT_SKY), then
+    restarted with the same command.  As in the reference (jobcore.c:100-104,
+    init.c:885-907, and the candidates it admits losing at jobcore.c:171):
+    the candidates buffered before the crash are lost, the run resumes at the
+    recorded sky point, and the final trigger file equals the uninterrupted
+    run's records from that sky point on; the state file is emptied at the
+    end."""
+    import subprocess
+    from polgraw_gb300 import build
+    data = str(tmp_path / "data")
+    os.makedirs(data)
+    m = materialize(case_by_name("h1l1_gaps_veto"), data)
+    name = "triggers_001_0200_1.bin"
+
+    def run(cwd, env=None):
+        os.makedirs(cwd, exist_ok=True)
+        e = dict(os.environ)
+        e.update(env or {})
+        return subprocess.run([build.EXE] + m["args"] + ["-output", os.path.join(cwd, "out")], cwd=cwd,
+                              capture_output=True, text=True, timeout=600, env=e)
+
+    full = str(tmp_path / "full")
+    r = run(full)
+    assert r.returncode == 0, r.stderr[-2000:]
+    A = np.fromfile(os.path.join(full, "out", name), dtype="<f8").reshape(-1, 5)
+    crash = str(tmp_path / "crash")
+    r = run(crash, {"PA_HOST_STOP_AT_SKY": "4"})
+    assert r.returncode == 3, (r.returncode, r.stderr[-2000:])
+    st = open(os.path.join(crash, "state_001_0200.dat")).read().split()
+    assert len(st) == 5                                   # pm mm nn sst FNum of the 4th sky point
+    assert not os.path.exists(os.path.join(crash, "out", name))   # nothing flushed before the crash
+    r = run(crash)                                        # restart: resumes from the state file
+    assert r.returncode == 0, r.stderr[-2000:]
+    C = np.fromfile(os.path.join(crash, "out", name), dtype="<f8").reshape(-1, 5)
+    assert 0 < len(C) < len(A)
+    assert np.array_equal(C, A[len(A) - len(C):])        # the tail of the uninterrupted run
+    lost = A[:len(A) - len(C)]
+    assert not ({tuple(x) for x in lost[:, 2:4]} & {tuple(x) for x in C[:, 2:4]})   # whole sky points lost
+    assert os.path.getsize(os.path.join(crash, "state_001_0200.dat")) == 0
