@@ -25,7 +25,7 @@ INCLUDE = os.path.join(ROOT, "include")
 CU_SOURCES = ["csrc/pa_engine_f32.cu", "csrc/pa_engine_f32_f64phase.cu", "csrc/pa_engine_f32_ffphase.cu",
               "csrc/pa_engine_f64.cu", "csrc/pa_api.cu", "csrc/pa_followup.cu", "csrc/pa_coinc.cu"]
 C_SOURCES = ["host/pa_host.c", "host/pa_coinc_host.c", "host/pa_grid.c"]
-HEADERS = ["csrc/pa_fft.cuh", "csrc/pa_engine.cuh", "csrc/pa_engine.h"]
+HEADERS = ["csrc/pa_fft.cuh", "csrc/pa_engine.cuh", "csrc/pa_engine.h", "csrc/pa_trace.h"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE]
 CC_FLAGS = ["-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-result",

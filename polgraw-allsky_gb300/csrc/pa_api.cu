@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/polgraw_gb300.h"
+#include "pa_trace.h"
 #include "pa_engine.h"
 
 #define SQR(x) ((x) * (x))
@@ -361,6 +362,7 @@ const char* pa_last_error(const pa_ctx* ctx) { return ctx ? ctx->err.c_str() : g
 
 pa_ctx* pa_create(const pa_settings* sett, const pa_detector* det, int nifo, const pa_config* cfg,
                   int* status) {
+  pa::TraceRange trace_("pa_create");
   char why[256];
   int st = PA_OK;
   if (!sett || !det) {
@@ -408,6 +410,7 @@ pa_ctx* pa_create(const pa_settings* sett, const pa_detector* det, int nifo, con
 }
 
 int pa_set_data(pa_ctx* c, const pa_detector* det, int nifo) {
+  pa::TraceRange trace_("pa_set_data");
   if (!c || !det || nifo != c->nifo) return fail(c, PA_ERR_ARG, "pa_set_data: bad arguments");
   CK(cudaSetDevice(c->dev), "cudaSetDevice");
   for (int n = 0; n < nifo; n++)
@@ -695,6 +698,7 @@ int graph_exec_from(cudaGraph_t g, cudaGraphExec_t* exec, std::string* err) {
 // launches that.  The timing event ev0 goes on the stream right before the
 // work (after the capture and graph update, which are host work).
 int launch_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
+  pa::TraceRange trace_("launch (capture, graph launch)");
   const bool graph = c->graphs && !c->prof.on;
   if (!graph) {
     CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
@@ -733,6 +737,7 @@ int launch_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
 // order, into `out`; returns PA_ERR_CAPACITY (with *n the count) when the
 // device buffer overflowed.
 int collect_tasks(pa_ctx* c, std::vector<pa::DevCand>* out, int* n_out) {
+  pa::TraceRange trace_("collect candidates");
   CK(cudaMemcpyAsync(c->h_ncand, c->b.ncand, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "copy count");
   CK(cudaStreamSynchronize(c->stream), "search");
   const int n = *c->h_ncand;
@@ -852,6 +857,7 @@ extern "C" {
 
 int pa_job_core(pa_ctx* c, int pm, int mm, int nn, const pa_opts* o, const pa_range* r, int* sgnlc,
                 double* sgnlv, int cap, pa_cand_idx* idx, int* FNum, int* needed) {
+  pa::TraceRange trace_("pa_job_core");
   if (!c || !o || !r || !sgnlc || !sgnlv || !FNum || cap < 0) return fail(c, PA_ERR_ARG, "pa_job_core: bad arguments");
   pa_sky t{pm, mm, nn};
   return pa_search_batch(c, &t, 1, o, r, sgnlc, sgnlv, cap, idx, FNum, needed);
@@ -859,6 +865,7 @@ int pa_job_core(pa_ctx* c, int pm, int mm, int nn, const pa_opts* o, const pa_ra
 
 int pa_search_batch(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o, const pa_range* r,
                     int* sgnlc, double* sgnlv, int cap, pa_cand_idx* idx, int* FNum, int* needed) {
+  pa::TraceRange trace_("pa_search_batch");
   if (!c || !tasks || ntasks < 0 || !o || !r || !sgnlc || !sgnlv || !FNum || cap < 0)
     return fail(c, PA_ERR_ARG, "pa_search_batch: bad arguments");
   if (needed) *needed = *sgnlc;
@@ -902,6 +909,7 @@ int pa_get_schedule(const pa_ctx* c, int* sbatch, int* split, int* max_sbatch) {
 
 int pa_autotune(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o, const pa_range* r, int* sbatch,
                 int* split) {
+  pa::TraceRange trace_("pa_autotune");
   if (!c || !tasks || ntasks < 1 || !o || !r) return fail(c, PA_ERR_ARG, "pa_autotune: bad arguments");
   std::vector<SkyHost> hs(ntasks);
   for (int t = 0; t < ntasks; t++)
@@ -1396,6 +1404,7 @@ int pa_segments_set_graph(pa_segments* sg, int on) {
 double pa_segments_last_call_ms(const pa_segments* sg) { return sg ? sg->last_ms : 0.; }
 
 int pa_segments_search(pa_segments* sg, const pa_segment_job* jobs, int* status) {
+  pa::TraceRange trace_("pa_segments_search");
   if (!sg || !jobs) return seg_fail(sg, PA_ERR_ARG, "pa_segments_search: bad arguments");
   const int ns = (int)sg->ctx.size();
   for (int k = 0; k < ns; k++) {

@@ -42,6 +42,7 @@
 #include <vector>
 
 #include "../../include/polgraw_gb300.h"
+#include "pa_trace.h"
 
 namespace {
 
@@ -988,6 +989,7 @@ static long long scan_tmp_len(long long n) {
 
 template <typename K>
 static int radix_sort(pa_coinc* c, K*& k, unsigned*& v, K* k2, unsigned* v2, long long n, int bits) {
+  pa::TraceRange trace_("coinc radix sort");
   const int nblk = (int)((n + kRTile - 1) / kRTile);
   ENS(hist, sizeof(unsigned) * (256ll * nblk + 1));
   ENS(cntl, sizeof(unsigned) * 256ll * nblk);
@@ -1138,6 +1140,7 @@ int pa_coinc_reset(pa_coinc* c) {
 }
 
 int pa_coinc_add_frame(pa_coinc* c, int frame, const double* records, long long n) {
+  pa::TraceRange trace_("pa_coinc_add_frame");
   if (!c || n < 0 || (n > 0 && !records)) return PA_ERR_ARG;
   if ((int)c->frames.size() >= kMaxFrames) return cfail(c, PA_ERR_ARG, "pa_coinc_add_frame: more than %d frames", kMaxFrames);
   if (c->nraw + n >= (1ll << 31)) return cfail(c, PA_ERR_ARG, "pa_coinc_add_frame: more than 2^31 records");
@@ -1175,6 +1178,7 @@ int pa_coinc_add_frame(pa_coinc* c, int frame, const double* records, long long 
 
 template <typename K>
 static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<long long>& nin_f) {
+  pa::TraceRange trace_("coinc sort, duplicates, coincidences");
   const int nf = (int)c->frames.size();
   const long long n = c->n_in;
   ENS(snr_in, sizeof(double) * n);
@@ -1447,6 +1451,7 @@ static int run_keyed(pa_coinc* c, const KeyLayout& L, int nblk1, std::vector<lon
 extern "C" {
 
 int pa_coinc_run(pa_coinc* c, pa_coinc_summary* sum) {
+  pa::TraceRange trace_("pa_coinc_run");
   if (!c) return PA_ERR_ARG;
   CCK(cudaSetDevice(c->cfg.device), "cudaSetDevice");
   const int nf = (int)c->frames.size();

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "../../include/polgraw_gb300.h"
+#include "pa_trace.h"
 
 namespace {
 
@@ -776,6 +777,7 @@ extern "C" {
 
 pa_followup* pa_followup_create(const pa_settings* sett, const pa_detector* det, int nifo, const pa_config* cfg,
                                 int* status) {
+  pa::TraceRange trace_("pa_followup_create");
   auto ret = [&](int st) {
     if (status) *status = st;
     return (pa_followup*)nullptr;
@@ -882,6 +884,7 @@ double pa_followup_last_call_ms(const pa_followup* f) { return f ? f->last_ms : 
 long long pa_followup_kernel_launches(const pa_followup* f) { return f ? f->launches : 0; }
 
 int pa_fstatnet(pa_followup* f, const double* sgnlo, int n, double* out) {
+  pa::TraceRange trace_("pa_fstatnet");
   if (!f || !sgnlo || !out || n < 0) return fu_fail(f, PA_ERR_ARG, "pa_fstatnet: invalid arguments");
   if (n == 0) return PA_OK;
   f->last_ms = 0.;
@@ -894,6 +897,7 @@ int pa_fstatnet(pa_followup* f, const double* sgnlo, int n, double* out) {
 }
 
 int pa_fstatnet_grad(pa_followup* f, const double* sgnlo, int n, const double* seed, double* F, double* grad) {
+  pa::TraceRange trace_("pa_fstatnet_grad");
   if (!f || !sgnlo || !F || !grad || n < 0) return fu_fail(f, PA_ERR_ARG, "pa_fstatnet_grad: invalid arguments");
   if (n == 0) return PA_OK;
   f->last_ms = 0.;
@@ -909,6 +913,7 @@ int pa_fstatnet_grad(pa_followup* f, const double* sgnlo, int n, const double* s
 }
 
 int pa_followup_ascent(pa_followup* f, double* sgnlo, int n, const pa_ascent_opts* opts, double* out, int* iters) {
+  pa::TraceRange trace_("pa_followup_ascent");
   if (!f || !sgnlo || !out || !opts || n < 0) return fu_fail(f, PA_ERR_ARG, "pa_followup_ascent: invalid arguments");
   for (int j = 0; j < 4; j++)
     if (!(opts->scale[j] > 0.)) return fu_fail(f, PA_ERR_ARG, "pa_followup_ascent: scale[%d] must be > 0", j);
@@ -1032,6 +1037,7 @@ void sx_propose(Simplex& S, double scale) {
 
 extern "C" int pa_followup_simplex(pa_followup* f, double* sgnlo, int n, const double* pc2, double tol,
                                    int max_evals, double* out, int* nevals) {
+  pa::TraceRange trace_("pa_followup_simplex");
   if (!f || !sgnlo || !pc2 || !out || n < 0) return fu_fail(f, PA_ERR_ARG, "pa_followup_simplex: invalid arguments");
   if (n == 0) return PA_OK;
   std::vector<Simplex> S(n);
