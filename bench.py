@@ -368,7 +368,7 @@ def run_segments(args, L):
         res_fixed = seg.search(tl, ol, rl)
         t_fixed += seg.last_call_ms()
     t0 = time.perf_counter()
-    sched = [c.autotune(g["tasks"][:4], g["opts"], g["range"]) for c, g in zip(ctxs, segs)]
+    sched = [c.autotune(g["tasks"][:4], g["opts"], g["range"]) + (c.lanes(),) for c, g in zip(ctxs, segs)]
     t_tune = time.perf_counter() - t0
     seg.set_graph(True)
     for _ in range(args.warmup):
@@ -591,7 +591,8 @@ def main():
     ap.add_argument("--fp64-sky", type=int, default=48, help="sky points timed in the all-FP64 form")
     ap.add_argument("--cpu-sky", type=int, default=48, help="sky points in the CPU-baseline sample")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--schedule", default="", help="fixed spindown schedule 'sbatch,split' (skips the autotuner)")
+    ap.add_argument("--schedule", default="",
+                    help="fixed spindown schedule 'sbatch,split[,lanes]' (lanes 1 when omitted; skips the autotuner)")
     ap.add_argument("--segments", type=int, default=24, help="segments workload: number of segments")
     ap.add_argument("--coinc-frames", type=int, default=24, help="coincidences workload: frames")
     ap.add_argument("--coinc-records", type=int, default=1 << 20, help="coincidences workload: records per frame")
@@ -682,12 +683,15 @@ def main():
     opts, rng = host.opts(), host.range
     templates = len(tasks) * nspin * bins
     if args.schedule:
-        sb_, sp_ = (int(v) for v in args.schedule.split(","))
-        ctx.set_schedule(sb_, sp_)
+        sv = [int(v) for v in args.schedule.split(",")]
+        ctx.set_lanes(1)
+        ctx.set_schedule(sv[0], sv[1])
+        ctx.set_lanes(sv[2] if len(sv) > 2 else 1)
     elif args.autotune:
         ctx.autotune(tasks[:8], opts, rng)
     ctx.set_graphs(bool(args.graphs))
     sched = ctx.schedule()
+    lanes = ctx.lanes()
     for _ in range(args.warmup):
         ctx.search_batch(tasks, opts, rng)
     launches0 = ctx.launches()
@@ -726,11 +730,13 @@ def main():
            "clocks": clk, "gpu_launches": int(launches),
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "candidates_per_step": ncand,
-           "schedule": {"spindown_batch": sched[0], "fft_split": sched[1],
+           "schedule": {"spindown_batch": sched[0], "fft_split": sched[1], "lanes": lanes,
                         "autotuned": bool(args.autotune) and not args.schedule}}
 
     if not args.no_extras and rank == 0:
-        # per-kernel CUDA-event profile of one step (not the timed number)
+        # per-kernel CUDA-event profile of one step (not the timed number; the
+        # context runs one spindown lane while profiling, so that each launch's
+        # events time that kernel alone)
         ctx.set_profiling(True)
         ctx.profile_reset()
         l2_flush()

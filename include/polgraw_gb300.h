@@ -234,19 +234,32 @@ int pa_profile_get(const pa_ctx *ctx, int kind, const char **name, double *total
 int pa_set_graphs(pa_ctx *ctx, int on);
 
 /* Spindown-loop schedule: spindowns per fused launch (1 .. *max_sbatch, the
- * batch the buffers were sized for, twice the automatic default) and the
+ * batch the buffers were sized for, four times the automatic default; a
+ * batch above *max_sbatch / 2 selects one lane, see pa_set_lanes) and the
  * factor split of the spindown FFT (0: L1 = 2^ceil(m/2), the default; 1:
  * swapped factors, different radix schedule of the two passes; for odd
  * m = log2(nfftf) only, ignored otherwise). */
 int pa_set_schedule(pa_ctx *ctx, int sbatch, int split);
 int pa_get_schedule(const pa_ctx *ctx, int *sbatch, int *split, int *max_sbatch);
 
-/* Times the candidate schedules (four spindown batches, 1/4 .. 4/4 of the
- * maximum, x the possible splits) on the given sky points (each searched
- * three times, the first as warm-up, CUDA-event device time) and keeps the
- * fastest; returns it in
- * *sbatch, *split (either may be NULL).  Results do not depend on sbatch;
- * the split changes FFT rounding only. */
+/* Spindown lanes: 1 (every spindown launch on the context's main stream) or
+ * 2 (consecutive spindown launches alternate between two streams, each with
+ * its own half of the FFT intermediate and F buffers, so that one launch's
+ * FFT passes run beside the previous launch's).  Two lanes need a spindown
+ * batch of at most *max_sbatch / 2 (PA_ERR_ARG otherwise: set the batch
+ * first).  Default: 2 when the configured batch allows it, else 1.  Results
+ * are identical either way; while the per-launch profile is on, one lane is
+ * used. */
+int pa_set_lanes(pa_ctx *ctx, int lanes);
+int pa_get_lanes(const pa_ctx *ctx, int *lanes);
+
+/* Times the candidate schedules (one lane with spindown batches of 1/4 ..
+ * 4/4 of the maximum, two lanes with 1/4 and 1/2, each x the possible
+ * splits) on the given sky points (each searched three times, the first as
+ * warm-up, CUDA-event device time) and keeps the fastest; returns it in
+ * *sbatch, *split (either may be NULL; the lane count it picked is read
+ * with pa_get_lanes).  Results do not depend on sbatch or the lanes; the
+ * split changes FFT rounding only. */
 int pa_autotune(pa_ctx *ctx, const pa_sky *tasks, int ntasks, const pa_opts *opts, const pa_range *s_range,
                 int *sbatch, int *split);
 

@@ -45,7 +45,9 @@ struct pa_ctx {
   int dev = 0;
   cudaStream_t stream = nullptr;      // spindown loop, copies
   cudaStream_t stream_pre = nullptr;  // per-sky preludes
+  cudaStream_t stream2 = nullptr;     // spindown lane 1
   cudaEvent_t ev_pre[2] = {nullptr, nullptr}, ev_spin[2] = {nullptr, nullptr};
+  cudaEvent_t ev_spin2[2] = {nullptr, nullptr};  // lane 1's last reads of each prelude slot
   pa::Buffers b;
   std::vector<void*> allocs;
   Twiddles tw_fwd, tw_inv, tw_invh, tw_main;
@@ -61,9 +63,17 @@ struct pa_ctx {
   // updated in place when the next batch has the same launch structure)
   bool graphs = false;
   std::vector<cudaGraphExec_t> gexec_parts;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
   int sb_max = 0;  // spindown batch the buffers are sized for
+  // spindown lanes: 1, or 2 (consecutive batches alternate between the main
+  // stream and stream2, each with its own half of ybuf and F, so that one
+  // batch's FFT passes run beside the previous batch's)
+  int lanes = 2;
 };
+
+// Lanes used by the next enqueue: one while the per-launch profile is on, so
+// that each kernel's events time that kernel alone.
+static int active_lanes(const pa_ctx* c) { return c->prof.on ? 1 : c->lanes; }
 
 // sky points per captured part of a batch (launch_tasks)
 constexpr size_t kGraphPart = 256;
@@ -240,9 +250,11 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   CK(cudaSetDevice(c->dev), "cudaSetDevice");
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
   CK(cudaStreamCreateWithFlags(&c->stream_pre, cudaStreamNonBlocking), "cudaStreamCreate");
+  CK(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking), "cudaStreamCreate");
   for (int k = 0; k < 2; k++) {
     CK(cudaEventCreateWithFlags(&c->ev_pre[k], cudaEventDisableTiming), "cudaEventCreate");
     CK(cudaEventCreateWithFlags(&c->ev_spin[k], cudaEventDisableTiming), "cudaEventCreate");
+    CK(cudaEventCreateWithFlags(&c->ev_spin2[k], cudaEventDisableTiming), "cudaEventCreate");
   }
   pa::Buffers& b = c->b;
   memset(&b, 0, sizeof(b));
@@ -263,9 +275,13 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
     sb = (int)std::max<size_t>(1, std::min<size_t>(64, ((size_t)64 << 20) / per));
   }
   b.sbatch = sb;
-  // buffers for up to twice the batch, for the schedule tuner
-  c->sb_max = std::min(128, 2 * sb);
+  // buffers for up to four times the batch, for the schedule tuner: one lane
+  // of up to sb_max spindowns, or two of up to sb_max / 2
+  c->sb_max = std::min(128, 4 * sb);
   const int sbm = c->sb_max;
+  b.lane_sb = sbm / 2;
+  // two lanes by default (measured 3% faster than one on H1+L1 N=86164)
+  c->lanes = sb <= b.lane_sb ? 2 : 1;
   const size_t rs = c->rsz, cs = 2 * c->rsz;
   int rc;
 #define ALLOC(ptr, bytes)                              \
@@ -342,6 +358,7 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   CK(cudaEventCreate(&c->ev1), "cudaEventCreate");
   CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
   CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "cudaEventCreate");
+  CK(cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming), "cudaEventCreate");
   return PA_OK;
 }
 
@@ -424,6 +441,7 @@ void pa_destroy(pa_ctx* c) {
   cudaSetDevice(c->dev);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->stream_pre) cudaStreamSynchronize(c->stream_pre);
+  if (c->stream2) cudaStreamSynchronize(c->stream2);
   delete c->eng;
   for (int i = 0; i < c->prof.cap; i++) {
     cudaEventDestroy(c->prof.recs[i].a);
@@ -434,15 +452,18 @@ void pa_destroy(pa_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_join2) cudaEventDestroy(c->ev_join2);
   drop_graphs(c);
   for (void* p : c->allocs) cudaFree(p);
   if (c->h_cand) cudaFreeHost(c->h_cand);
   if (c->h_ncand) cudaFreeHost(c->h_ncand);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->stream_pre) cudaStreamDestroy(c->stream_pre);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
   for (int k = 0; k < 2; k++) {
     if (c->ev_pre[k]) cudaEventDestroy(c->ev_pre[k]);
     if (c->ev_spin[k]) cudaEventDestroy(c->ev_spin[k]);
+    if (c->ev_spin2[k]) cudaEventDestroy(c->ev_spin2[k]);
   }
   delete c;
 }
@@ -612,30 +633,45 @@ pa::SkyArgs sky_args(const pa_ctx* c, const SkyHost& h, int task) {
 
 // Enqueues one sky point: its prelude on the prelude stream into slot
 // task % 2 (after the spindowns that last read that slot), and its spindown
-// batches on the main stream (after the prelude).
+// batches after the prelude, on the main stream or, with two lanes,
+// alternately on the main stream and stream2 (*lane: the lane of the next
+// batch, carried over from sky point to sky point).
 int enqueue_sky(pa_ctx* c, const SkyHost& h, const pa_opts* o, int task, void* Fdbg, int Fss,
-                bool wait_slot = true) {
+                bool wait_slot = true, int* lane = nullptr) {
   const pa::SkyArgs a = sky_args(c, h, task);
   const int slot = task & 1;
-  if (wait_slot) CK(cudaStreamWaitEvent(c->stream_pre, c->ev_spin[slot], 0), "cudaStreamWaitEvent");
+  const int lanes = Fdbg ? 1 : active_lanes(c);
+  if (wait_slot) {
+    CK(cudaStreamWaitEvent(c->stream_pre, c->ev_spin[slot], 0), "cudaStreamWaitEvent");
+    // (the debug path is never captured: it may wait on lane 1's reads of an
+    // earlier call too)
+    if (lanes == 2 || Fdbg) CK(cudaStreamWaitEvent(c->stream_pre, c->ev_spin2[slot], 0), "cudaStreamWaitEvent");
+  }
   cudaError_t e = c->eng->prelude(a, slot, c->stream_pre);
   if (e != cudaSuccess) return cuda_fail(c, e, "prelude launch");
   CK(cudaEventRecord(c->ev_pre[slot], c->stream_pre), "cudaEventRecord");
   CK(cudaStreamWaitEvent(c->stream, c->ev_pre[slot], 0), "cudaStreamWaitEvent");
+  if (lanes == 2) CK(cudaStreamWaitEvent(c->stream2, c->ev_pre[slot], 0), "cudaStreamWaitEvent");
   if (Fdbg) {
-    e = c->eng->spindowns(a, slot, Fss, 1, o->trl, o->white_flag, o->s0_flag, c->stream, Fdbg);
+    e = c->eng->spindowns(a, slot, 0, Fss, 1, o->trl, o->white_flag, o->s0_flag, c->stream, Fdbg);
     if (e != cudaSuccess) return cuda_fail(c, e, "spindown launch");
   } else {
     // full launches and one remainder: splitting into equal launches (200 as
     // 4 x 50 instead of 3 x 64 + 8) was measured 1.5% slower, as each
     // launch's last partial wave of CTAs costs a whole wave
+    int l0 = 0;
+    int* ln = lane ? lane : &l0;
     for (int ss = h.smin; ss <= h.smax; ss += c->b.sbatch) {
       const int nb = std::min(c->b.sbatch, h.smax - ss + 1);
-      e = c->eng->spindowns(a, slot, ss, nb, o->trl, o->white_flag, o->s0_flag, c->stream, nullptr);
+      const int l = lanes == 2 ? *ln : 0;
+      e = c->eng->spindowns(a, slot, l, ss, nb, o->trl, o->white_flag, o->s0_flag, l ? c->stream2 : c->stream,
+                            nullptr);
       if (e != cudaSuccess) return cuda_fail(c, e, "spindown launch");
+      if (lanes == 2) *ln ^= 1;
     }
   }
   CK(cudaEventRecord(c->ev_spin[slot], c->stream), "cudaEventRecord");
+  if (lanes == 2) CK(cudaEventRecord(c->ev_spin2[slot], c->stream2), "cudaEventRecord");
   return PA_OK;
 }
 
@@ -655,19 +691,26 @@ bool cand_less(const pa::DevCand& x, const pa::DevCand& y) {
 // starts).  Works unchanged under stream capture.
 int enqueue_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o, size_t t0, size_t t1,
                   bool reset) {
+  const int lanes = active_lanes(c);
   if (reset) CK(cudaMemsetAsync(c->b.ncand, 0, sizeof(int), c->stream), "memset");
   CK(cudaEventRecord(c->ev_fork, c->stream), "cudaEventRecord");
   CK(cudaStreamWaitEvent(c->stream_pre, c->ev_fork, 0), "cudaStreamWaitEvent");
+  if (lanes == 2) CK(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0), "cudaStreamWaitEvent");
   bool used[2] = {false, false};
+  int lane = 0;
   for (size_t t = t0; t < t1; t++) {
     if (!hs[t].inside || hs[t].nss == 0) continue;
     const int slot = (int)t & 1;
-    int rc = enqueue_sky(c, hs[t], o, (int)t, nullptr, 0, used[slot]);
+    int rc = enqueue_sky(c, hs[t], o, (int)t, nullptr, 0, used[slot], &lane);
     if (rc) return rc;
     used[slot] = true;
   }
   CK(cudaEventRecord(c->ev_join, c->stream_pre), "cudaEventRecord");
   CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "cudaStreamWaitEvent");
+  if (lanes == 2) {
+    CK(cudaEventRecord(c->ev_join2, c->stream2), "cudaEventRecord");
+    CK(cudaStreamWaitEvent(c->stream, c->ev_join2, 0), "cudaStreamWaitEvent");
+  }
   return PA_OK;
 }
 
@@ -896,6 +939,30 @@ int pa_set_schedule(pa_ctx* c, int sbatch, int split) {
     return fail(c, PA_ERR_ARG, "pa_set_schedule: sbatch must be in [1, %d], split 0 or 1", c ? c->sb_max : 0);
   c->b.sbatch = sbatch;
   c->eng->set_split(split);
+  if (c->lanes == 2 && sbatch > c->b.lane_sb) {  // too large for a lane: one lane
+    CK(cudaSetDevice(c->dev), "cudaSetDevice");
+    drop_graphs(c);
+    c->lanes = 1;
+  }
+  return PA_OK;
+}
+
+int pa_set_lanes(pa_ctx* c, int lanes) {
+  if (!c || lanes < 1 || lanes > 2) return fail(c, PA_ERR_ARG, "pa_set_lanes: lanes must be 1 or 2");
+  if (lanes == 2 && c->b.sbatch > c->b.lane_sb)
+    return fail(c, PA_ERR_ARG, "pa_set_lanes: two lanes need a spindown batch of at most %d (now %d)",
+                c->b.lane_sb, c->b.sbatch);
+  if (lanes != c->lanes) {
+    CK(cudaSetDevice(c->dev), "cudaSetDevice");
+    drop_graphs(c);
+  }
+  c->lanes = lanes;
+  return PA_OK;
+}
+
+int pa_get_lanes(const pa_ctx* c, int* lanes) {
+  if (!c || !lanes) return PA_ERR_ARG;
+  *lanes = c->lanes;
   return PA_OK;
 }
 
@@ -914,23 +981,30 @@ int pa_autotune(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o, co
   std::vector<SkyHost> hs(ntasks);
   for (int t = 0; t < ntasks; t++)
     sky_setup(c, tasks[t].pm, tasks[t].mm, tasks[t].nn, o, t == 0 ? r->sst : r->spndr[0], r->spndr[1], &hs[t]);
-  const int sb0 = c->b.sbatch, sp0 = c->eng->split();
-  int cands[4] = {std::max(1, c->sb_max / 4), std::max(1, c->sb_max / 2), std::max(1, 3 * c->sb_max / 4),
-                  c->sb_max};
+  const int sb0 = c->b.sbatch, sp0 = c->eng->split(), ln0 = c->lanes;
+  // (lanes, spindown batch) candidates: one lane with a quarter to all of the
+  // buffers, two lanes with a quarter or half each
+  const int m = c->sb_max;
+  const int cands[6][2] = {{1, m / 4}, {1, m / 2}, {1, 3 * m / 4}, {1, m}, {2, m / 4}, {2, m / 2}};
   // the factor split is a choice only for odd log2(nfftf)
   const int nsplit = (c->sett.nfftf & 0xAAAAAAAA) ? 2 : 1;
   double best = 1e300;
-  int bsb = sb0, bsp = sp0;
+  int bsb = sb0, bsp = sp0, bln = ln0;
   std::vector<pa::DevCand> out;
-  for (int k = 0; k < 4; k++) {
-    if (k > 0 && cands[k] == cands[k - 1]) continue;
+  for (int k = 0; k < 6; k++) {
+    const int ln = cands[k][0], sb = std::max(1, cands[k][1]);
+    bool seen = false;
+    for (int q = 0; q < k; q++) seen = seen || (cands[q][0] == ln && std::max(1, cands[q][1]) == sb);
+    if (seen) continue;
     for (int sp = 0; sp < nsplit; sp++) {
-      c->b.sbatch = cands[k];
+      c->lanes = ln;
+      c->b.sbatch = sb;
       c->eng->set_split(sp);
       double t = 1e300;
       for (int rep = 0; rep < 3; rep++) {  // first run warms up
         int rc = run_tasks(c, hs, o, &out);
         if (rc) {
+          c->lanes = ln0;
           c->b.sbatch = sb0;
           c->eng->set_split(sp0);
           return rc;
@@ -939,11 +1013,13 @@ int pa_autotune(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o, co
       }
       if (t < best) {
         best = t;
-        bsb = cands[k];
+        bsb = sb;
         bsp = sp;
+        bln = ln;
       }
     }
   }
+  c->lanes = bln;
   c->b.sbatch = bsb;
   c->eng->set_split(bsp);
   drop_graphs(c);
@@ -1139,6 +1215,7 @@ size_t noalloc_layout(char* base, const pa_settings& s, int nifo, pa::Buffers* b
   b->nifo = nifo;
   b->fftpad = s.fftpad;
   b->sbatch = 1;
+  b->lane_sb = 1;
   b->cand_cap = kNoAllocCandCap;
   for (int k = 0; k < 4; k++) {
     b->tw_fwd[k] = tw[0][k];
@@ -1275,7 +1352,7 @@ extern "C" int pa_fstat_noalloc(const pa_settings* sett, const pa_detector* det,
   if (!eng) return noalloc_fail(PA_ERR_NOMEM, "pa_fstat_noalloc: engine storage too small");
   const pa::SkyArgs a = sky_args(&c, h, 0);
   e = eng->prelude(a, 0, st);
-  if (e == cudaSuccess) e = eng->spindowns(a, 0, ss, 1, o->trl, o->white_flag, o->s0_flag, st, Fn);
+  if (e == cudaSuccess) e = eng->spindowns(a, 0, 0, ss, 1, o->trl, o->white_flag, o->s0_flag, st, Fn);
   const int bins = sett->nmax - sett->nmin;
   if (e == cudaSuccess) e = cudaMemcpyAsync(g_noalloc_F, Fn, 4 * (size_t)bins, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

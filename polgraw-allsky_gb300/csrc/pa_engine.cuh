@@ -1075,8 +1075,11 @@ template <typename R, int PM> class EngineT : public Engine {
     return cudaGetLastError();
   }
 
-  cudaError_t spindowns(const SkyArgs& sky, int slot, int ss0, int nb, double trl, int white, int s0_flag,
-                        cudaStream_t st, void* Fdbg) override {
+  cudaError_t spindowns(const SkyArgs& sky, int slot, int lane, int ss0, int nb, double trl, int white,
+                        int s0_flag, cudaStream_t st, void* Fdbg) override {
+    const size_t lo = (size_t)lane * b_.lane_sb;  // first spindown of the lane in ybuf and F
+    T* const yb = (T*)b_.ybuf + lo * 2 * b_.nfftf;
+    R* const Fl = (R*)b_.F + lo * b_.bins;
     SpinLoader<R, PM> sl;
     sl.xm = (const T*)b_.xm[slot];
     sl.ph0 = b_.ph0[slot];
@@ -1089,12 +1092,12 @@ template <typename R, int PM> class EngineT : public Engine {
     sl.M4 = sky.M4;
     sl.M5 = sky.M5;
     sl.s1_0 = sky.s1_0;
-    FstatStore<R> fs{(R*)b_.F, (const R*)b_.sums_r[slot], b_.nmin, b_.nmax, b_.bins};
-    cudaError_t e = fft<-1, true>(gm_, b_.tw_main, sl, fs, nb, st, KK_SPIN_A, KK_SPIN_B, b_.ybuf, split_);
+    FstatStore<R> fs{Fl, (const R*)b_.sums_r[slot], b_.nmin, b_.nmax, b_.bins};
+    cudaError_t e = fft<-1, true>(gm_, b_.tw_main, sl, fs, nb, st, KK_SPIN_A, KK_SPIN_B, yb, split_);
     if (e != cudaSuccess) return e;
     const int nchunk = (b_.bins + 4095) / 4096;
     pre(KK_THRESHOLD, nb, st);
-    k_normthresh<R><<<dim3(nchunk, nb), 256, 0, st>>>((const R*)b_.F, b_.bins, b_.nblk, white, (R)trl,
+    k_normthresh<R><<<dim3(nchunk, nb), 256, 0, st>>>(Fl, b_.bins, b_.nblk, white, (R)trl,
                                                       b_.nmin, ss0, sky.task, b_.cand, b_.ncand,
                                                       b_.cand_cap, (R*)Fdbg);
     post(st);

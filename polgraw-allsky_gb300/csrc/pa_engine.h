@@ -76,8 +76,10 @@ struct Buffers {
   double* part;                     // partial sums of a^2, b^2
   void* ybuf_pre;                   // FFT intermediate of the prelude, nifo*2*Ninterp
   unsigned int* counter;            // CTA completion counter of the prelude (kept 0)
-  void* ybuf;                       // FFT intermediate of the spindown loop, sbatch*2*nfftf
-  void* F;                          // [sbatch][bins] Real
+  void* ybuf;                       // FFT intermediate of the spindown loop, 2*lane_sb*2*nfftf
+  void* F;                          // [2*lane_sb][bins] Real
+  int lane_sb;                      // spindowns per lane of ybuf and F: lane 1 starts at
+                                    // spindown lane_sb (two lanes run on two streams)
   void* mu;                         // [sbatch][nblk] Real
   DevCand* cand;
   int* ncand;
@@ -117,11 +119,12 @@ class Engine {
   // Enqueues the per-sky prelude (jobcore.c:270-393) on `st`, outputs to
   // prelude slot `slot`.
   virtual cudaError_t prelude(const SkyArgs& sky, int slot, cudaStream_t st) = 0;
-  // Enqueues spindowns ss0 .. ss0+nb-1 (nb <= sbatch) reading prelude slot
-  // `slot`: phase modulation, FFT, F-statistic, normalisation, threshold
-  // and candidate compaction.  Fdbg (optional): normalised F of the batch,
-  // [nb][bins] Real.
-  virtual cudaError_t spindowns(const SkyArgs& sky, int slot, int ss0, int nb, double trl, int white,
+  // Enqueues spindowns ss0 .. ss0+nb-1 reading prelude slot `slot` into
+  // lane `lane` of ybuf and F (lane 0: nb <= 2*lane_sb; lane 1, which starts
+  // at spindown lane_sb of the buffers: nb <= lane_sb): phase modulation, FFT,
+  // F-statistic, normalisation, threshold and candidate compaction.  Fdbg
+  // (optional): normalised F of the batch, [nb][bins] Real.
+  virtual cudaError_t spindowns(const SkyArgs& sky, int slot, int lane, int ss0, int nb, double trl, int white,
                                 int s0_flag, cudaStream_t st, void* Fdbg) = 0;
   virtual long long launches() const = 0;
   virtual size_t real_size() const = 0;

@@ -30,8 +30,8 @@ EXPORTS = [
     "pa_host_create", "pa_host_setup", "pa_host_search", "pa_host_main", "pa_host_destroy",
     "pa_host_settings", "pa_host_detectors", "pa_host_range", "pa_host_core_opts",
     "pa_host_config", "pa_host_detector_name",
-    "pa_set_graphs", "pa_set_schedule", "pa_get_schedule", "pa_autotune", "pa_segments_create",
-    "pa_segments_destroy", "pa_segments_last_error", "pa_segments_set_graph", "pa_segments_search",
+    "pa_set_graphs", "pa_set_schedule", "pa_get_schedule", "pa_set_lanes", "pa_get_lanes", "pa_autotune",
+    "pa_segments_create", "pa_segments_destroy", "pa_segments_last_error", "pa_segments_set_graph", "pa_segments_search",
     "pa_segments_last_call_ms",
     "pa_followup_create", "pa_followup_destroy", "pa_followup_last_error", "pa_fstatnet", "pa_fstatnet_grad",
     "pa_followup_ascent", "pa_followup_simplex", "pa_followup_last_call_ms", "pa_followup_kernel_launches",
@@ -137,6 +137,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.pa_set_graphs.argtypes = [C.c_void_p, C.c_int]
     lib.pa_set_schedule.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.pa_get_schedule.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int)]
+    lib.pa_set_lanes.argtypes = [C.c_void_p, C.c_int]
+    lib.pa_get_lanes.argtypes = [C.c_void_p, P(C.c_int)]
     lib.pa_autotune.argtypes = [C.c_void_p, P(Sky), C.c_int, P(Opts), P(Range), P(C.c_int), P(C.c_int)]
     lib.pa_segments_create.restype = C.c_void_p
     lib.pa_segments_create.argtypes = [P(C.c_void_p), C.c_int, P(C.c_int)]
@@ -385,6 +387,16 @@ class Context:
         a, b, m = C.c_int(0), C.c_int(0), C.c_int(0)
         self.lib.pa_get_schedule(self.ctx, C.byref(a), C.byref(b), C.byref(m))
         return a.value, b.value, m.value
+
+    def set_lanes(self, lanes: int):
+        rc = self.lib.pa_set_lanes(self.ctx, lanes)
+        if rc != PA_OK:
+            raise SearchError("pa_set_lanes failed (%d): %s" % (rc, self.error()))
+
+    def lanes(self) -> int:
+        n = C.c_int(0)
+        self.lib.pa_get_lanes(self.ctx, C.byref(n))
+        return n.value
 
     def autotune(self, tasks, opts: Opts, rng: Range):
         arr = (Sky * len(tasks))(*[Sky(*t) for t in tasks])

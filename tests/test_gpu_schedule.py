@@ -3,7 +3,9 @@ them may change the search's results.
 
 * graphs on/off: identical records and indices, also when the graph is
   updated in place for a second batch of the same shape;
-* spindown batch sizes: identical results; the swapped FFT factor split
+* spindown batch sizes: identical results; two spindown lanes (launches
+  alternating between two streams): identical results, with and without
+  graphs, and the lane/batch limits rejected; the swapped FFT factor split
   (odd log2(nfftf)): the reference's candidates within the usual tolerance;
 * pa_autotune: picks a valid schedule, results still match the reference;
 * pa_segments_search over contexts of different N (one per golden case),
@@ -67,6 +69,39 @@ def test_spindown_batch_sizes_identical(tmp_path, gpu_ok):
         _same(ref, _batch(ctx, host))
 
 
+@pytest.mark.parametrize("graphs", [False, True])
+def test_two_lanes_identical(graphs, tmp_path, gpu_ok):
+    from polgraw_gb300.lib import SearchError
+    host, _ = make_host(case_by_name("h1l1_gaps_veto"), str(tmp_path))
+    ctx = _ctx(host)
+    sb, split, sbmax = ctx.schedule()
+    assert ctx.lanes() == 2            # the default when the batch fits a lane
+    ctx.set_lanes(1)
+    ref = _batch(ctx, host)
+    ctx.set_graphs(graphs)
+    ctx.set_schedule(sbmax, split)
+    with pytest.raises(SearchError):
+        ctx.set_lanes(2)               # the batch is larger than one lane
+    assert ctx.lanes() == 1
+    for b in sorted({1, 3, sbmax // 2}):
+        ctx.set_schedule(b, split)
+        ctx.set_lanes(2)
+        assert ctx.lanes() == 2
+        _same(ref, _batch(ctx, host))
+        _same(ref, _batch(ctx, host))  # graph replay / second call
+        ctx.set_lanes(1)
+    ctx.set_lanes(2)
+    ctx.set_schedule(sbmax, split)     # too large for a lane: one lane
+    assert ctx.lanes() == 1
+    _same(ref, _batch(ctx, host))
+    with pytest.raises(SearchError):
+        ctx.set_lanes(3)
+    # the per-launch profile runs one lane and still gives the same records
+    ctx.set_profiling(True)
+    _same(ref, _batch(ctx, host))
+    ctx.set_profiling(False)
+
+
 def _golden_match(name, rec, idx, host, rtol=1e-4):
     g = golden(name)
     ref = g["candidates"]
@@ -99,6 +134,7 @@ def test_autotune(tmp_path, gpu_ok):
     sb, split = ctx.autotune(pts, host.opts(), host.range)
     s2, sp2, smax = ctx.schedule()
     assert (sb, split) == (s2, sp2) and 1 <= sb <= smax and split in (0, 1)
+    assert ctx.lanes() in (1, 2) and (ctx.lanes() == 1 or sb <= smax // 2)
     rec, idx, _ = _batch(ctx, host)
     assert _golden_match(name, rec, idx, host) > 0
 
