@@ -18,6 +18,8 @@
 #pragma once
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "pa_engine.h"
 #include "pa_fft.cuh"
@@ -419,6 +421,131 @@ template <typename R, int PM> struct SpinLoader {
     va = mk(accx, accy);
     vb = mk(bccx, bccy);
   }
+
+  // One detector's term of load2 (FP32 forms, n < N): xm_{a,b,d}[n] times
+  // exp(-i phase_d(n)), with the phase evaluated as load2 does.
+  __device__ __forceinline__ void mod1(int d, int n, T& pa, T& pb, const char* sm) const {
+    static_assert(sizeof(R) == 4, "FP32 forms only");
+    const SpinCta* p = reinterpret_cast<const SpinCta*>(sm);
+    const size_t o = (size_t)d * N + n;
+    const float4 lo16 = __ldg(reinterpret_cast<const float4*>(xm) + 2 * o);
+    const uint4 hi16 = __ldg(reinterpret_cast<const uint4*>(xm) + 2 * o + 1);
+    float sn, cs;
+    if (PM == PM_FIXED) {
+      const uint64_t A = ((uint64_t)hi16.y << 32) | hi16.x;
+      const uint64_t B = ((uint64_t)hi16.w << 32) | hi16.z;
+      const uint64_t t = A + mul64x32(B, p->ssr) + mul64x32(p->H, (unsigned)n);
+      const float x = (float)(int)(t >> 32) * 4.656612873077393e-10f;  // 2^-31
+      sincospif(x, &sn, &cs);
+    } else if (PM == PM_F64) {
+      const double t1 = __longlong_as_double((long long)(((unsigned long long)hi16.y << 32) | hi16.x));
+      const double ph = fma(p->s1, t1, p->het1 * (double)n);
+      const double kk = rint(ph * kInvTwoPi);
+      double r = fma(-kk, kTwoPiHi, ph);
+      r = fma(-kk, kTwoPiLo, r);
+      sincosf((float)r, &sn, &cs);
+    } else {
+      const float2 tt = make_float2(__uint_as_float(hi16.x), __uint_as_float(hi16.y));
+      float p1 = p->s1h * tt.x;
+      float e1 = fmaf(p->s1h, tt.x, -p1);
+      e1 = fmaf(p->s1h, tt.y, e1);
+      e1 = fmaf(p->s1l, tt.x, e1);
+      const float nf = (float)n;
+      float p2 = p->h1h * nf;
+      float e2 = fmaf(p->h1h, nf, -p2);
+      e2 = fmaf(p->h1l, nf, e2);
+      const float s = p1 + p2;
+      const float bb = s - p1;
+      const float err = (p1 - (s - bb)) + (p2 - bb);
+      const float e = err + e1 + e2;
+      const float kk = rintf(s * kInvTwoPiF);
+      float r = fmaf(-kk, kTwoPiF_A, s);
+      r = fmaf(-kk, kTwoPiF_B, r);
+      r = fmaf(-kk, kTwoPiF_C, r);
+      r += e;
+      sincosf(r, &sn, &cs);
+    }
+    pa = mk(lo16.x * cs + lo16.y * sn, lo16.y * cs - lo16.x * sn);
+    pb = mk(lo16.z * cs + lo16.w * sn, lo16.w * cs - lo16.z * sn);
+  }
+};
+
+// Spindown pass A for two detectors and L1 = 256 = 16 x 16 (the FP32 forms):
+// the column FFTs of k_pass_a as two radix-16 stages with one barrier
+// between them, each thread holding 16 values of one array.
+//   stage 1: warp w = b (n1 mod 16), lane = 2 col + arr.  At the 16 positions
+//     n1 = 16 a + b of column col the thread evaluates detector arr's term
+//     (mod1) and swaps with its partner lane (lane ^ 1) the term of the array
+//     the partner keeps, so that it holds x_arr = term_0 + term_1: one sincos
+//     per detector and position, as the paired loader.  16-point DFT over a,
+//     twiddle W_256^{b c}, store Z[c][b].
+//   stage 2: warp = column, lane = 2 c + arr.  16-point DFT over b gives
+//     Y[k1 = c + 16 d]; inter-pass twiddle W_L^{n2 k1}; stored like k_pass_a
+//     (the a|b values of one (n2, k1) adjacent, 256 contiguous bytes per warp).
+// Shared tile: Z[c][b][lane] at c * 514 + b * 32 + lane (float2); the pad of
+// 2 per c makes the stage-2 reads conflict-free (half-warp slots 2c + arr).
+template <int SIGN, int LOGL, int PM>
+__global__ void __launch_bounds__(512, 2)
+    k_pass_a16(const SpinLoader<float, PM> ld, const float2* __restrict__ tw1, const float2* __restrict__ twlo,
+               const float2* __restrict__ twhi, float2* __restrict__ ybuf) {
+  constexpr int LOGL1 = 8, LOGL2 = LOGL - LOGL1, ZC = 16 * 32 + 2;
+  constexpr int Lmask = (1 << LOGL) - 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* z = reinterpret_cast<float2*>(smem_raw);
+  float2* tws = z + 16 * ZC;
+  char* lsm = reinterpret_cast<char*>(tws + 256);
+  const int batch = blockIdx.y;
+  const int c0 = blockIdx.x << 4;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int m = threadIdx.x; m < 256; m += 512) tws[m] = tw1[m];
+  ld.prologue(batch, lsm);
+  __syncthreads();
+  float2 v[16];
+  {
+    const int arr = lane & 1;
+    const int n2 = c0 + (lane >> 1);
+#pragma unroll
+    for (int a = 0; a < 16; ++a) {
+      const int n = ((16 * a + w) << LOGL2) + n2;
+      float2 pa = make_float2(0.f, 0.f), pb = pa;
+      if (n < ld.N) ld.mod1(arr, n, pa, pb, lsm);
+      const float2 send = arr ? pa : pb;
+      const float2 mine = arr ? pb : pa;
+      const float rx = __shfl_xor_sync(0xffffffffu, send.x, 1);
+      const float ry = __shfl_xor_sync(0xffffffffu, send.y, 1);
+      v[a] = make_float2(mine.x + rx, mine.y + ry);
+    }
+    dft16<SIGN>(v);
+#pragma unroll
+    for (int c = 1; c < 16; ++c) v[c] = cmul(v[c], tws[w * c]);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) z[c * ZC + w * 32 + lane] = v[c];
+  }
+  __syncthreads();
+  {
+    const int arr = lane & 1, c = lane >> 1;
+    const int n2 = c0 + w;
+#pragma unroll
+    for (int b = 0; b < 16; ++b) v[b] = z[c * ZC + b * 32 + 2 * w + arr];
+    dft16<SIGN>(v);
+    float2* yb = ybuf + ((size_t)batch << (LOGL + 1)) + ((size_t)n2 << (LOGL1 + 1)) + arr;
+#pragma unroll
+    for (int d = 0; d < 16; ++d) {
+      const int k1 = c + 16 * d;
+      const int m = (n2 * k1) & Lmask;
+      const float2 W = cmul(__ldg(&twlo[m & 1023]), __ldg(&twhi[m >> 10]));
+      yb[2 * k1] = cmul(v[d], W);
+    }
+  }
+}
+
+template <class L> struct IsSpinF32 {
+  static constexpr bool value = false;
+  static constexpr int pm = 0;
+};
+template <int PM> struct IsSpinF32<SpinLoader<float, PM>> {
+  static constexpr bool value = true;
+  static constexpr int pm = PM;
 };
 
 // Complex output with a scale factor (resampling FFTs).
@@ -944,6 +1071,9 @@ template <typename R, int PM> class EngineT : public Engine {
   Geom gf_, gm_;
   long long launches_ = 0;
   int split_ = 0;
+  // spindown pass A of two detectors with L1 = 256: the radix-16 kernel
+  // (default) or the generic radix-4/8 one (environment PA_SPIN_PASS_A=radix8)
+  bool a16_ = true;
 
   // CUDA events around a launch when profiling is on
   void pre(int kind, int items, cudaStream_t st) {
@@ -989,7 +1119,19 @@ template <typename R, int PM> class EngineT : public Engine {
     smem_attr(kb, G::smem_b, doneB);
     dim3 ga(G::L2 >> G::LOGC, batch), gb(G::L1 >> G::LOGRR, batch);
     pre(kind_a, batch, stream);
-    ka<<<ga, NT, G::smem_a, stream>>>(ld, t1, tlo, thi, yb);
+    bool done = false;
+    if constexpr (IsSpinF32<Loader>::value && G::LOGL1 == 8 && G::C == 16 && NT == 512) {
+      // two detectors, L1 = 256: the two-stage radix-16 pass A
+      if (ld.nifo == 2 && a16_) {
+        auto k16 = k_pass_a16<SIGN, LOGL, IsSpinF32<Loader>::pm>;
+        constexpr int smem16 = (16 * (16 * 32 + 2) + 256) * (int)sizeof(float2) + 128;
+        static bool done16 = false;
+        smem_attr(k16, smem16, done16);
+        k16<<<ga, 512, smem16, stream>>>(ld, t1, tlo, thi, yb);
+        done = true;
+      }
+    }
+    if (!done) ka<<<ga, NT, G::smem_a, stream>>>(ld, t1, tlo, thi, yb);
     post(stream);
     pre(kind_b, batch, stream);
     kb<<<gb, NT, G::smem_b, stream>>>(st, t2, yb);
@@ -1019,6 +1161,8 @@ template <typename R, int PM> class EngineT : public Engine {
 
  public:
   explicit EngineT(const Buffers& b) : b_(b) {
+    const char* pa = getenv("PA_SPIN_PASS_A");
+    a16_ = !(pa && strcmp(pa, "radix8") == 0);
     gf_ = make_geom(b.nfft, TileCfg<R>::E);
     gm_ = make_geom(b.nfftf, TileCfg<R>::E);
   }

@@ -90,6 +90,50 @@ template <int SIGN, class T> __device__ __forceinline__ void dft8(T* v) {
   v[7] = csub(e3, t3);
 }
 
+// x * exp(SIGN 2 pi i e / 16) for a compile-time e in 1 .. 9
+template <int SIGN, int e, class T> __device__ __forceinline__ T w16(T x) {
+  typedef decltype(x.x) R;
+  if (e == 4) return mulj<SIGN>(x);
+  // cos and sin of 2 pi e / 16 for e = 0 .. 9
+  constexpr double kc[10] = {1., 0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173, 0.,
+                             -0.38268343236508977173, -0.70710678118654752440, -0.92387953251128675613, -1.,
+                             -0.92387953251128675613};
+  constexpr double ks[10] = {0., 0.38268343236508977173, 0.70710678118654752440, 0.92387953251128675613, 1.,
+                             0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173, 0.,
+                             -0.38268343236508977173};
+  const R c = (R)kc[e], s = (R)(SIGN * ks[e]);
+  return mk(x.x * c - x.y * s, x.x * s + x.y * c);
+}
+
+// 16-point DFT in natural order, as 4 x 4: X[k1 + 4 k2] =
+// sum_n2 W4^{n2 k2} W16^{n2 k1} sum_n1 x[4 n1 + n2] W4^{n1 k1}
+template <int SIGN, class T> __device__ __forceinline__ void dft16(T* v) {
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft4<SIGN>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+  // v[n2 + 4 k1] now holds the inner transform (n2, k1)
+  v[5] = w16<SIGN, 1>(v[5]);
+  v[6] = w16<SIGN, 2>(v[6]);
+  v[7] = w16<SIGN, 3>(v[7]);
+  v[9] = w16<SIGN, 2>(v[9]);
+  v[10] = w16<SIGN, 4>(v[10]);
+  v[11] = w16<SIGN, 6>(v[11]);
+  v[13] = w16<SIGN, 3>(v[13]);
+  v[14] = w16<SIGN, 6>(v[14]);
+  v[15] = w16<SIGN, 9>(v[15]);
+  T o[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    T a = v[4 * k1], b = v[4 * k1 + 1], c = v[4 * k1 + 2], d = v[4 * k1 + 3];
+    dft4<SIGN>(a, b, c, d);
+    o[k1] = a;
+    o[k1 + 4] = b;
+    o[k1 + 8] = c;
+    o[k1 + 12] = d;
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = o[k];
+}
+
 template <int SIGN, int RAD, class T> __device__ __forceinline__ void dftr(T* v) {
   if (RAD == 2) dft2<SIGN>(v);
   else if (RAD == 4) dft4v<SIGN>(v);

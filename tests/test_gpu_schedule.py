@@ -102,6 +102,30 @@ def test_two_lanes_identical(graphs, tmp_path, gpu_ok):
     ctx.set_profiling(False)
 
 
+@pytest.mark.parametrize("name", ["h1l1_gaps_veto", "h1l1_white_pm2", "h1l1_gridgen"])
+def test_pass_a_radix16_agrees_with_radix8(name, tmp_path, gpu_ok, monkeypatch):
+    """Two detectors with L1 = 256 take the two-stage radix-16 spindown pass A;
+    the generic radix-4/8 kernel (PA_SPIN_PASS_A=radix8) gives the same
+    candidates, F within FP32 rounding."""
+    host, _ = make_host(case_by_name(name), str(tmp_path))
+    monkeypatch.setenv("PA_SPIN_PASS_A", "radix8")
+    c8 = _ctx(host)
+    monkeypatch.delenv("PA_SPIN_PASS_A")
+    c16 = _ctx(host)
+    for split in (0, 1):
+        c8.set_schedule(c8.schedule()[0], split)
+        c16.set_schedule(c16.schedule()[0], split)
+        r8, i8, f8 = _batch(c8, host)
+        r16, i16, f16 = _batch(c16, host)
+        assert f8 == f16
+        F = lambda snr: snr * snr / 2 + 2  # noqa: E731
+        matched, err, bad = compare_candidates(key_of(i8), [F(r[4]) for r in r8], key_of(i16),
+                                               [F(r[4]) for r in r16], host.opts().trl, 1e-5)
+        assert not bad and err <= 1e-5 and matched > 0, (split, bad[:5], err)
+    c8.close()
+    c16.close()
+
+
 def _golden_match(name, rec, idx, host, rtol=1e-4):
     g = golden(name)
     ref = g["candidates"]
