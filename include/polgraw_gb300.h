@@ -236,9 +236,11 @@ int pa_set_graphs(pa_ctx *ctx, int on);
 /* Spindown-loop schedule: spindowns per fused launch (1 .. *max_sbatch, the
  * batch the buffers were sized for, four times the automatic default; a
  * batch above *max_sbatch / 2 selects one lane, see pa_set_lanes) and the
- * factor split of the spindown FFT (0: L1 = 2^ceil(m/2), the default; 1:
- * swapped factors, different radix schedule of the two passes; for odd
- * m = log2(nfftf) only, ignored otherwise). */
+ * factor split of the spindown FFT (0: L1 = 2^ceil(m/2); 1: swapped
+ * factors, different radix schedule of the two passes; for odd
+ * m = log2(nfftf) only, ignored otherwise; default 0, except 1 for two
+ * detectors in the FP32 forms with nfftf = 2^17, whose 256-point columns
+ * take the radix-16 pass A). */
 int pa_set_schedule(pa_ctx *ctx, int sbatch, int split);
 int pa_get_schedule(const pa_ctx *ctx, int *sbatch, int *split, int *max_sbatch);
 

@@ -354,6 +354,9 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   c->eng = c->fp64 ? pa::make_engine_f64(b) : pa::make_engine_f32(b, c->cfg.phase_mode);
   if (!c->eng) return fail(c, PA_ERR_NOMEM, "engine allocation failed");
   c->eng->prof = &c->prof;
+  // default factor split: for two detectors in the FP32 forms, the one with
+  // 256-point columns (the radix-16 spindown pass A): swapped for nfftf = 2^17
+  if (!c->fp64 && nifo == 2 && s.nfftf == (1 << 17)) c->eng->set_split(1);
   CK(cudaEventCreate(&c->ev0), "cudaEventCreate");
   CK(cudaEventCreate(&c->ev1), "cudaEventCreate");
   CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
