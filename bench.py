@@ -735,8 +735,8 @@ def main():
 
     if not args.no_extras and rank == 0:
         # per-kernel CUDA-event profile of one step (not the timed number; the
-        # context runs one spindown lane while profiling, so that each launch's
-        # events time that kernel alone)
+        # context runs its kernels one at a time while profiling, so that each
+        # launch's events time that kernel alone, as ncu's serialised list)
         ctx.set_profiling(True)
         ctx.profile_reset()
         l2_flush()

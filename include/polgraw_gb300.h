@@ -212,7 +212,10 @@ double pa_last_call_ms(const pa_ctx *ctx);
 
 /* Per-kernel profile: when on, every kernel launch of the context is
  * bracketed by CUDA events on its stream and its duration accumulated per
- * kernel kind (adds a small overhead; off by default). */
+ * kernel kind (adds a small overhead; off by default).  While it is on the
+ * context runs its kernels one at a time (the preludes on the main stream,
+ * one spindown lane, no graphs), so that each duration is that kernel's
+ * own; the records are the same. */
 int pa_set_profiling(pa_ctx *ctx, int on);
 void pa_profile_reset(pa_ctx *ctx);
 /* Totals of kernel kind `kind` (0, 1, ...); returns PA_ERR_ARG past the

@@ -71,9 +71,11 @@ struct pa_ctx {
   int lanes = 2;
 };
 
-// Lanes used by the next enqueue: one while the per-launch profile is on, so
-// that each kernel's events time that kernel alone.
+// Lanes used by the next enqueue, and the stream of the preludes: while the
+// per-launch profile is on, one lane and the preludes on the main stream, so
+// that every kernel runs alone and its events time that kernel only.
 static int active_lanes(const pa_ctx* c) { return c->prof.on ? 1 : c->lanes; }
+static cudaStream_t prelude_stream(const pa_ctx* c) { return c->prof.on ? c->stream : c->stream_pre; }
 
 // sky points per captured part of a batch (launch_tasks)
 constexpr size_t kGraphPart = 256;
@@ -644,15 +646,16 @@ int enqueue_sky(pa_ctx* c, const SkyHost& h, const pa_opts* o, int task, void* F
   const pa::SkyArgs a = sky_args(c, h, task);
   const int slot = task & 1;
   const int lanes = Fdbg ? 1 : active_lanes(c);
+  cudaStream_t sp = prelude_stream(c);
   if (wait_slot) {
-    CK(cudaStreamWaitEvent(c->stream_pre, c->ev_spin[slot], 0), "cudaStreamWaitEvent");
+    CK(cudaStreamWaitEvent(sp, c->ev_spin[slot], 0), "cudaStreamWaitEvent");
     // (the debug path is never captured: it may wait on lane 1's reads of an
     // earlier call too)
-    if (lanes == 2 || Fdbg) CK(cudaStreamWaitEvent(c->stream_pre, c->ev_spin2[slot], 0), "cudaStreamWaitEvent");
+    if (lanes == 2 || Fdbg) CK(cudaStreamWaitEvent(sp, c->ev_spin2[slot], 0), "cudaStreamWaitEvent");
   }
-  cudaError_t e = c->eng->prelude(a, slot, c->stream_pre);
+  cudaError_t e = c->eng->prelude(a, slot, sp);
   if (e != cudaSuccess) return cuda_fail(c, e, "prelude launch");
-  CK(cudaEventRecord(c->ev_pre[slot], c->stream_pre), "cudaEventRecord");
+  CK(cudaEventRecord(c->ev_pre[slot], sp), "cudaEventRecord");
   CK(cudaStreamWaitEvent(c->stream, c->ev_pre[slot], 0), "cudaStreamWaitEvent");
   if (lanes == 2) CK(cudaStreamWaitEvent(c->stream2, c->ev_pre[slot], 0), "cudaStreamWaitEvent");
   if (Fdbg) {
