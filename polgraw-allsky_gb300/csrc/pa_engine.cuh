@@ -21,6 +21,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
+
 #include "pa_engine.h"
 #include "pa_fft.cuh"
 
@@ -1071,6 +1073,7 @@ template <typename R, int PM> class EngineT : public Engine {
   Geom gf_, gm_;
   long long launches_ = 0;
   int split_ = 0;
+  int dev_ = 0;  // device the engine was made on (current at construction)
   // spindown pass A of two detectors with L1 = 256: the radix-16 kernel
   // (default) or the generic radix-4/8 one (environment PA_SPIN_PASS_A=radix8)
   bool a16_ = true;
@@ -1091,11 +1094,14 @@ template <typename R, int PM> class EngineT : public Engine {
     prof->n++;
   }
 
-  // opt-in above 48 KB of dynamic shared memory, once per kernel instance
-  template <class K> static void smem_attr(K kernel, int bytes, bool& done) {
-    if (!done) {
+  // opt-in above 48 KB of dynamic shared memory, once per kernel instance and
+  // device (the attribute is set on the current device: the engine's own,
+  // made current by every entry point); `done` holds one bit per device
+  template <class K> void smem_attr(K kernel, int bytes, std::atomic<unsigned long long>& done) const {
+    const unsigned long long bit = 1ull << (dev_ & 63);
+    if (!(done.load(std::memory_order_acquire) & bit)) {
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-      done = true;
+      done.fetch_or(bit, std::memory_order_release);
     }
   }
 
@@ -1114,7 +1120,7 @@ template <typename R, int PM> class EngineT : public Engine {
     T* yb = (T*)ybuf;
     auto ka = k_pass_a<R, SIGN, LOGL, Loader, SPLIT>;
     auto kb = k_pass_b<R, SIGN, LOGL, Storer, SPLIT>;
-    static bool doneA = false, doneB = false;
+    static std::atomic<unsigned long long> doneA{0}, doneB{0};
     smem_attr(ka, G::smem_a, doneA);
     smem_attr(kb, G::smem_b, doneB);
     dim3 ga(G::L2 >> G::LOGC, batch), gb(G::L1 >> G::LOGRR, batch);
@@ -1125,7 +1131,7 @@ template <typename R, int PM> class EngineT : public Engine {
       if (ld.nifo == 2 && a16_) {
         auto k16 = k_pass_a16<SIGN, LOGL, IsSpinF32<Loader>::pm>;
         constexpr int smem16 = (16 * (16 * 32 + 2) + 256) * (int)sizeof(float2) + 128;
-        static bool done16 = false;
+        static std::atomic<unsigned long long> done16{0};
         smem_attr(k16, smem16, done16);
         k16<<<ga, 512, smem16, stream>>>(ld, t1, tlo, thi, yb);
         done = true;
@@ -1161,6 +1167,7 @@ template <typename R, int PM> class EngineT : public Engine {
 
  public:
   explicit EngineT(const Buffers& b) : b_(b) {
+    cudaGetDevice(&dev_);
     const char* pa = getenv("PA_SPIN_PASS_A");
     a16_ = !(pa && strcmp(pa, "radix8") == 0);
     gf_ = make_geom(b.nfft, TileCfg<R>::E);
@@ -1200,7 +1207,7 @@ template <typename R, int PM> class EngineT : public Engine {
     constexpr int W = SplineCfg<R>::warm;
     const int smf = spad_len<R>(kSplineSeg) * (int)sizeof(double2) + spad_len<R>(kSplineSeg + W + 2) * (int)sizeof(T);
     const int smb = spad_len<R>(kSplineSeg + W) * (int)sizeof(double2) + spad_len<R>(kSplineSeg) * (int)sizeof(T);
-    static bool donef = false, doneb = false;
+    static std::atomic<unsigned long long> donef{0}, doneb{0};
     smem_attr(k_spline_fwd<R>, smf, donef);
     smem_attr(k_spline_bwd<R>, smb, doneb);
     pre(KK_SPLINE_FWD, nifo, st);
