@@ -136,8 +136,8 @@ int pa_set_data(pa_ctx *ctx, const pa_detector *det, int nifo);
 
 void pa_destroy(pa_ctx *ctx);
 
-/* Last error message of the context (or of the last failed pa_create when
- * ctx is NULL). */
+/* Last error message of the context (or, with ctx NULL, of this thread's
+ * last failed pa_create). */
 const char *pa_last_error(const pa_ctx *ctx);
 
 /* Drop-in for job_core() (jobcore.c:189-785).
@@ -437,6 +437,8 @@ int pa_coinc_vedva(const double *fisher, double *vedva);
 
 pa_coinc *pa_coinc_create(const pa_coinc_cfg *cfg, int *status);
 void pa_coinc_destroy(pa_coinc *cc);
+/* Last error message of the handle (or, with cc NULL, of this thread's last
+ * failed pa_coinc_create). */
 const char *pa_coinc_last_error(const pa_coinc *cc);
 /* Starts a new set of frames (keeps the device buffers). */
 int pa_coinc_reset(pa_coinc *cc);

@@ -876,7 +876,7 @@ struct pa_coinc {
   bool ev1_done = false;                 // the run's end event is already on the stream
 };
 
-static std::string g_coinc_create_error;
+thread_local std::string g_coinc_create_error;  // per host thread, as the other create errors
 
 enum CoincKind { CK_CELLS = 0, CK_INBAND, CK_SORT_HIST, CK_SORT_SCATTER, CK_SCAN, CK_FRAME_RANK, CK_DEDUP,
                  CK_COMPACT, CK_GROUPS, CK_MEANS, CK_COUNT };
