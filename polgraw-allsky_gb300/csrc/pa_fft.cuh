@@ -159,6 +159,12 @@ template <> struct Pair<float2> {
     a = make_float2(v.x, v.y);
     b = make_float2(v.z, v.w);
   }
+  // last read of the data: evict-first
+  __device__ __forceinline__ static void ldlast(const float2* p, float2& a, float2& b) {
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(p));
+    a = make_float2(v.x, v.y);
+    b = make_float2(v.z, v.w);
+  }
   __device__ __forceinline__ static void st(float2* p, float2 a, float2 b) {
     *reinterpret_cast<float4*>(p) = make_float4(a.x, a.y, b.x, b.y);
   }
@@ -172,6 +178,10 @@ template <> struct Pair<double2> {
   __device__ __forceinline__ static void ldg(const double2* p, double2& a, double2& b) {
     a = __ldg(p);
     b = __ldg(p + 1);
+  }
+  __device__ __forceinline__ static void ldlast(const double2* p, double2& a, double2& b) {
+    a = __ldcs(p);
+    b = __ldcs(p + 1);
   }
   __device__ __forceinline__ static void st(double2* p, double2 a, double2 b) {
     p[0] = a;
@@ -385,8 +395,9 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
   const int k10 = blockIdx.x << G::LOGRR;
   for (int m = threadIdx.x; m < G::L2; m += NT) tws[m] = tw2[m];
   const T* yb = ybuf + ((size_t)batch << (LOGL + 1));
+  // the intermediate is read once, here: evict-first
   auto src = [&](int n2, int rr, T& a, T& b) {
-    Pair<T>::ldg(yb + (((size_t)n2 << G::LOGL1) + k10 + rr) * 2, a, b);
+    Pair<T>::ldlast(yb + (((size_t)n2 << G::LOGL1) + k10 + rr) * 2, a, b);
   };
   __syncthreads();
   fft_front<SIGN, E, NT, G::LOGL2, G::LOGRR, P>(s, tws, src);
