@@ -536,8 +536,8 @@ def coinc_extra(L, steps: int = 3) -> dict:
 
 
 def followup_extra(L, steps: int = 3) -> dict:
-    """The followup F-statistic (demodulated, BASELINE config 5 shape: H1+L1+V1,
-    N=86164, 4096 candidates) and its adjoint gradient, device time per batch
+    """The followup F-statistic (demodulated; H1+L1+V1, N=86164, 4096
+    candidates) and its adjoint gradient, device time per batch
     in the default mixed form (FP64 phase) and with the two-float phase."""
     tmp = tempfile.mkdtemp(prefix="pa_followup_")
     argv, inj = workloads.followup(tmp)

@@ -4,7 +4,7 @@ Two things are built here:
 
 * ``oracle/_build/liboracle.so`` -- the all-FP64 C restatement of the
   reference hot path (oracle.c + fft.c), OpenMP-parallel over spindowns.  It is
-  the parity checker for the CUDA library and the timed CPU baseline ("port")
+  the parity reference for the CUDA library and the timed CPU baseline ("port")
   of bench.py.  Built from this repository's sources on any machine.
 
 * ``oracle/_ref/`` -- the UNMODIFIED reference search compiled from its own

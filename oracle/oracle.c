@@ -1,7 +1,8 @@
 /*
  * oracle/oracle.c -- all-FP64 CPU restatement of the reference coherent
- * search hot path.  TEST INFRASTRUCTURE ONLY (see oracle.h): the checker for
- * the CUDA library and the timed CPU baseline ("port") of bench.py.
+ * search hot path.  TEST INFRASTRUCTURE ONLY (see oracle.h): the parity
+ * reference for the CUDA library and the timed CPU baseline ("port") of
+ * bench.py.
  *
  * Each function follows the reference file:line named in its comment, with
  * the same floating-point expression order (the build uses

@@ -2,8 +2,8 @@
  * oracle/oracle.h -- CPU oracle for the coherent network search hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C, all-FP64 restatement of the
- * reference's job_core() and the helpers it calls.  It is the checker for
- * the CUDA library: only the tests, the smoke check and the CPU-baseline leg
+ * reference's job_core() and the helpers it calls.  It is the parity
+ * reference for the CUDA library: only the tests, the smoke check and the CPU-baseline leg
  * of bench.py load it.  The product never links or calls it.
  *
  * Parity is pinned by comparing this oracle's candidates against the

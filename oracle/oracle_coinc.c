@@ -4,7 +4,7 @@
  * coincidences/src/coincidences.c:117-600 and the transformation matrix of
  * manage_grid_matrix() (search/network/src-cpu/init.c:1142-1210).
  *
- * TEST INFRASTRUCTURE ONLY: the checker of pa_coinc_* (only tests/ and
+ * TEST INFRASTRUCTURE ONLY: the parity reference of pa_coinc_* (only tests/ and
  * bench.py's CPU leg load it).  Plain sequential C, FP64 without FMA
  * contraction (built with -ffp-contract=off), so that every cell index and
  * every mean is the value the reference computes on x86-64.

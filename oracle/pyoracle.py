@@ -1,7 +1,8 @@
 """ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, as the checker.  The product never uses it.
+CPU-baseline leg of bench.py, as the parity reference.  The product never
+uses it.
 """
 from __future__ import annotations
 

@@ -6,7 +6,7 @@ shims) on deterministic synthetic inputs; here the oracle restatement runs
 on the same inputs through the product's C host set-up and must reproduce
 every candidate: indices exactly, f/s1/delta/alpha bit for bit (same FP64
 expressions), SNR to 1e-9 relative.  This pins the oracle that the GPU tests
-then use as their checker.
+then compare against.
 """
 import numpy as np
 import pytest
