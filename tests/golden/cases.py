@@ -18,6 +18,9 @@ Coverage (reference file:line of the behaviour each case exercises):
   h1l1_gridgen     a grid made by the reference grid generator (gridgen/) from
                    the synthetic ephemeris: lower-triangular M with frequency-
                    sky and frequency-spindown couplings (make_gridgen_grids.py)
+  h1l1v1_addsig    three detectors (H1, L1, V1: the detector sum of
+                   jobcore.c:471-623 and the weights of :374-393 over nifo=3),
+                   -addsig network injection, M4 != 0, lowered threshold
   cfg1_h1          the 1-detector N=86164 workload: 1 sky point (delta 0.3,
                    alpha 1.2) x 64 spindowns, injected f=0.1 fdot=-1e-8 SNR 12
 """
@@ -55,6 +58,11 @@ CASES = [
          inject=dict(f=1.3, fdot=0.0, delta=0.5, alpha=2.1, snr=20.0),
          range=[-2, 2, 0, 1, -4, -3, None, None],
          args=["-threshold", "16"]),
+    dict(name="h1l1v1_addsig",
+         data=dict(dets=["H1", "L1", "V1"], dt=8.0, nod=1, band=150, fftpad=1,
+                   grid=dict(m5=-2e-8, m4=2.9e-4, sky_scale=0.05)),
+         addsig=dict(f=1.7, fdot=-4.0e-8, delta=0.3, alpha=1.2, snr=14.0, gsize=2),
+         args=["-threshold", "12"]),
     dict(name="cfg1_h1",
          data=dict(dets=["H1"], dt=2.0, nod=2, band=666, fftpad=1,
                    grid=dict(m5=-1e-9, sky_point=(0.3, 1.2))),
