@@ -66,5 +66,13 @@ def materialize(case: dict, root: str) -> dict:
         path = os.path.join(root, "range.txt")
         synth.write_range(path, r[0:2], r[2:4], r[4:6], r[6:8])
         args += ["-range", path]
+    for det, rows in case.get("lines", {}).items():
+        # known-lines file read by read_lines() (settings.c:327-400): '%'
+        # comment lines, then frequency, type, offset, first and last comb
+        # index (and two unused columns) per line
+        with open(os.path.join(root, "O1LinesToBeCleaned_%s_v1.txt" % det), "w") as fh:
+            fh.write("%% known lines of %s\n" % det)
+            for r in rows:
+                fh.write("\t".join(repr(float(x)) if i in (0, 2) else str(int(x)) for i, x in enumerate(r)) + "\n")
     args += list(case.get("args", []))
     return {"args": args, "ds": ds, "pm": pm}

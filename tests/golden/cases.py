@@ -21,6 +21,12 @@ Coverage (reference file:line of the behaviour each case exercises):
   h1l1v1_addsig    three detectors (H1, L1, V1: the detector sum of
                    jobcore.c:471-623 and the weights of :374-393 over nifo=3),
                    -addsig network injection, M4 != 0, lowered threshold
+  h1v1_lines_usedet  three detectors on disk, -usedet H1V1 (init.c:150-152,
+                   detector selection), --vetolines (main.c:89-98) with
+                   known-lines files per detector
+                   (read_lines settings.c:327-400: types 0, 1 and 2, lines out
+                   of band, the unused detector's file ignored) merged into
+                   the band veto (lines_in_band, jobcore.c:675-684)
   cfg1_h1          the 1-detector N=86164 workload: 1 sky point (delta 0.3,
                    alpha 1.2) x 64 spindowns, injected f=0.1 fdot=-1e-8 SNR 12
 """
@@ -63,6 +69,15 @@ CASES = [
                    grid=dict(m5=-2e-8, m4=2.9e-4, sky_scale=0.05)),
          addsig=dict(f=1.7, fdot=-4.0e-8, delta=0.3, alpha=1.2, snr=14.0, gsize=2),
          args=["-threshold", "12"]),
+    dict(name="h1v1_lines_usedet",
+         data=dict(dets=["H1", "L1", "V1"], dt=8.0, nod=1, band=120, fftpad=1,
+                   grid=dict(m5=-1.5e-8, sky_scale=0.05)),
+         # band 120 at dt=8: fpo = 17.265625 Hz, width 0.0625 Hz
+         lines={"H1": [[17.28, 0, 0.0, 0, 0, 0, 0], [30.0, 0, 0.0, 0, 0, 0, 0]],
+                "L1": [[17.30, 0, 0.0, 0, 0, 0, 0]],
+                "V1": [[1.0, 1, 0.31, 15, 18, 0, 0], [8.6485, 2, 0.0, 2, 2, 0, 0]]},
+         range=[-4, 4, -1, 1, -1, 1, 1, 1],
+         args=["-threshold", "11", "-usedet", "H1V1", "--vetolines"]),
     dict(name="cfg1_h1",
          data=dict(dets=["H1"], dt=2.0, nod=2, band=666, fftpad=1,
                    grid=dict(m5=-1e-9, sky_point=(0.3, 1.2))),
