@@ -74,5 +74,13 @@ def materialize(case: dict, root: str) -> dict:
             fh.write("%% known lines of %s\n" % det)
             for r in rows:
                 fh.write("\t".join(repr(float(x)) if i in (0, 2) else str(int(x)) for i, x in enumerate(r)) + "\n")
+    if case.get("label"):
+        # -label: the reference reads xdatc_<ident>_<band>_<label>.bin
+        # (init.c:174-175, settings.c:134) and names its outputs with the label
+        for det in data["dets"]:
+            dd = os.path.join(root, "%03d" % 1, det)
+            os.rename(os.path.join(dd, "xdatc_%03d_%04d.bin" % (1, data["band"])),
+                      os.path.join(dd, "xdatc_%03d_%04d_%s.bin" % (1, data["band"], case["label"])))
+        args += ["-label", case["label"]]
     args += list(case.get("args", []))
     return {"args": args, "ds": ds, "pm": pm}

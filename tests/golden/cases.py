@@ -27,6 +27,9 @@ Coverage (reference file:line of the behaviour each case exercises):
                    (read_lines settings.c:327-400: types 0, 1 and 2, lines out
                    of band, the unused detector's file ignored) merged into
                    the band veto (lines_in_band, jobcore.c:675-684)
+  h1l1_label_pm2   -label (input xdatc_<ident>_<band>_<label>.bin, trigger
+                   and state file names, init.c:174-175, jobcore.c:92-93),
+                   second hemisphere only
   cfg1_h1          the 1-detector N=86164 workload: 1 sky point (delta 0.3,
                    alpha 1.2) x 64 spindowns, injected f=0.1 fdot=-1e-8 SNR 12
 """
@@ -78,6 +81,12 @@ CASES = [
                 "V1": [[1.0, 1, 0.31, 15, 18, 0, 0], [8.6485, 2, 0.0, 2, 2, 0, 0]]},
          range=[-4, 4, -1, 1, -1, 1, 1, 1],
          args=["-threshold", "11", "-usedet", "H1V1", "--vetolines"]),
+    dict(name="h1l1_label_pm2",
+         data=dict(dets=["H1", "L1"], dt=8.0, nod=1, band=90, fftpad=1,
+                   grid=dict(m5=-1.2e-8, sky_scale=0.05)),
+         label="O3a",
+         range=[-3, 3, -1, 1, -1, 0, 2, 2],
+         args=["-threshold", "11"]),
     dict(name="cfg1_h1",
          data=dict(dets=["H1"], dt=2.0, nod=2, band=666, fftpad=1,
                    grid=dict(m5=-1e-9, sky_point=(0.3, 1.2))),

@@ -62,7 +62,8 @@ def run_case(case: dict, exe: str) -> dict:
         ranges = [tuple(int(g) for g in mm.groups()) for mm in RANGE_RE.finditer(r.stdout)]
         recs = []
         for pm in (1, 2):
-            f = os.path.join(out, "triggers_001_%04d_%d.bin" % (case["data"]["band"], pm))
+            lbl = "_" + case["label"] if case.get("label") else ""
+            f = os.path.join(out, "triggers_001_%04d%s_%d.bin" % (case["data"]["band"], lbl, pm))
             if os.path.exists(f):
                 recs.append((pm, np.fromfile(f, dtype="<f8").reshape(-1, 5)))
         allrec = np.concatenate([x[1] for x in recs]) if recs else np.zeros((0, 5))
