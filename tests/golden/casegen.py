@@ -56,8 +56,8 @@ def materialize(case: dict, root: str) -> dict:
     if "addsig" in case:
         a = dict(case["addsig"])
         path = os.path.join(root, "addsig.txt")
-        synth.write_addsig(path, f=a["f"], fdot=a["fdot"], delta=a["delta"], alpha=a["alpha"], snr=a["snr"],
-                           gsize=a.get("gsize", 2), reffr=1)
+        synth.write_addsig(path, f=a["f"], fdot=a["fdot"], delta=a["delta"], alpha=a["alpha"], snr=a.get("snr"),
+                           amp=a.get("amp"), gsize=a.get("gsize", 2), reffr=1)
         args += ["-addsig", path]
     if "range" in case:
         r = list(case["range"])

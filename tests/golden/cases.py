@@ -30,6 +30,9 @@ Coverage (reference file:line of the behaviour each case exercises):
   h1l1_label_pm2   -label (input xdatc_<ident>_<band>_<label>.bin, trigger
                    and state file names, init.c:174-175, jobcore.c:92-93),
                    second hemisphere only
+  h1l1_amp_fpo     -addsig in the amplitude form ("amp h0 gsize reffr",
+                   init.c:488-490) with grid size 1; explicit -fpo, which
+                   places the known line of L1 in the band (lines_in_band)
   cfg1_h1          the 1-detector N=86164 workload: 1 sky point (delta 0.3,
                    alpha 1.2) x 64 spindowns, injected f=0.1 fdot=-1e-8 SNR 12
 """
@@ -87,6 +90,13 @@ CASES = [
          label="O3a",
          range=[-3, 3, -1, 1, -1, 0, 2, 2],
          args=["-threshold", "11"]),
+    dict(name="h1l1_amp_fpo",
+         data=dict(dets=["H1", "L1"], dt=8.0, nod=1, band=60, fftpad=1,
+                   grid=dict(m5=-2e-8, sky_scale=0.05)),
+         addsig=dict(f=2.2, fdot=-3e-8, delta=0.3, alpha=1.2, amp=0.25, gsize=1),
+         # with -fpo 20.0 the band is [20.0, 20.0625] Hz
+         lines={"L1": [[20.04, 0, 0.0, 0, 0, 0, 0]]},
+         args=["-threshold", "12", "-fpo", "20.0", "--vetolines"]),
     dict(name="cfg1_h1",
          data=dict(dets=["H1"], dt=2.0, nod=2, band=666, fftpad=1,
                    grid=dict(m5=-1e-9, sky_point=(0.3, 1.2))),
