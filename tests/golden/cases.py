@@ -111,12 +111,23 @@ CASES = [
 # Fstatnet() at points around the injection and runs its simplex (amoeba)
 # from offset starting points.
 #   fu_h1l1v1   three detectors (H1, L1, V1), N=10771 (1 day at dt=8 s)
+#   fu_h1l1_dt2 two detectors (H1, L1), N=43082 (1 day at dt=2 s), southern sky
 FOLLOWUP_CASES = [
     dict(name="fu_h1l1v1",
          data=dict(dets=["H1", "L1", "V1"], dt=8.0, nod=1, band=100, fftpad=1,
                    grid=dict(m5=-2e-8, sky_scale=0.05)),
          inject=dict(f=1.0, fdot=-6e-8, delta=0.3, alpha=1.2, snr=25.0),
-         range=[0, 0, 0, 0, 0, 0, None, None]),
+         range=[0, 0, 0, 0, 0, 0, None, None],
+         # no other maximum of F within 0.5 peak widths of the injection
+         unimodal=True),
+    dict(name="fu_h1l1_dt2",
+         data=dict(dets=["H1", "L1"], dt=2.0, nod=1, band=666, fftpad=1,
+                   grid=dict(m5=-1e-9, sky_scale=0.05)),
+         inject=dict(f=2.0, fdot=-2e-8, delta=-0.5, alpha=4.0, snr=20.0),
+         range=[0, 0, 0, 0, 0, 0, None, None],
+         # local maxima of F (about 151.6 and 102) lie within 0.5 peak widths
+         # of the peak (152.1): an ascent from a nearby start may stop there
+         unimodal=False),
 ]
 
 # Coincidence step (coincidences/src/coincidences.c) over synthetic trigger

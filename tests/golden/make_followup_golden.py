@@ -105,8 +105,10 @@ def run_case(case: dict) -> dict:
                              "built by oracle/build_oracle.py"}
 
 
-def main():
+def main(names=None):
     for case in FOLLOWUP_CASES:
+        if names and case["name"] not in names:
+            continue
         g = run_case(case)
         path = os.path.join(HERE, case["name"] + ".json")
         with open(path, "w") as f:
@@ -116,4 +118,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

@@ -21,11 +21,9 @@ pytestmark = pytest.mark.gpu
 FORMS = {"mixed": (0, 1e-4, 2e-3, 0), "mixed-ffphase": (0, 1e-4, 2e-3, 2), "fp64": (1, 1e-10, 1e-8, 0)}
 
 
-@pytest.fixture(scope="module")
-def fu_case(tmp_path_factory):
+def _load_case(case, tmp_path_factory):
     from polgraw_gb300.lib import Host
     from pyoracle import FollowupOracle
-    case = FOLLOWUP_CASES[0]
     g = golden(case["name"])
     tmp = tmp_path_factory.mktemp("fu")
     data = tmp / "data"
@@ -34,12 +32,22 @@ def fu_case(tmp_path_factory):
     assert m["ds"].files == g["inputs"], "synthetic inputs differ from the golden run's"
     host = Host(m["args"] + ["-output", str(tmp / "out"), "--nocheckpoint"])
     dets, nifo = host.detectors()
-    return host, dets, nifo, g, FollowupOracle(host.settings, dets, nifo)
+    return host, dets, nifo, g, FollowupOracle(host.settings, dets, nifo), case
+
+
+@pytest.fixture(scope="module", params=[c["name"] for c in FOLLOWUP_CASES])
+def fu_case(tmp_path_factory, request):
+    return _load_case([c for c in FOLLOWUP_CASES if c["name"] == request.param][0], tmp_path_factory)
+
+
+@pytest.fixture(scope="module")
+def fu_first_case(tmp_path_factory):
+    return _load_case(FOLLOWUP_CASES[0], tmp_path_factory)
 
 
 def _fu(fu_case, form):
     from polgraw_gb300.lib import Followup
-    host, dets, nifo, g, _ = fu_case
+    host, dets, nifo, g = fu_case[:4]
     return Followup(host.settings, dets, nifo, precision=FORMS[form][0], phase_mode=FORMS[form][3])
 
 
@@ -110,14 +118,14 @@ def test_adjoint_matches_finite_differences_fp64(fu_case, gpu_ok):
         assert np.abs(w * (grad[0] - fd)).max() <= 1e-5 * scale
 
 
-def test_autograd_function(fu_case, gpu_ok):
-    """The adjoint behind a torch.autograd.Function (test harness only): the
-    backward pass returns grad_output * dF/dtheta, the directional derivative
-    matches a central difference, and an optimiser step in peak-width units
-    raises F."""
+def test_autograd_function(fu_first_case, gpu_ok):
+    """The adjoint behind a torch.autograd.Function (test harness only; the
+    wrapper's plumbing, checked on the first followup case): the backward
+    pass returns grad_output * dF/dtheta, the directional derivative matches a
+    central difference, and an optimiser step in peak-width units raises F."""
     torch = pytest.importorskip("torch")
-    g = fu_case[3]
-    fu = _fu(fu_case, "mixed")
+    g = fu_first_case[3]
+    fu = _fu(fu_first_case, "mixed")
     w = torch.tensor(g["widths"], dtype=torch.float64)
 
     class Fstat(torch.autograd.Function):
@@ -136,7 +144,9 @@ def test_autograd_function(fu_case, gpu_ok):
     u = (pts / w).clone().requires_grad_(True)   # peak-width units
     F0 = Fstat.apply(u * w)
     F0.sum().backward()
-    _, grad = fu.fstatnet_grad(pts.numpy())
+    # the gradient at the points the forward pass evaluated ((pts / w) * w can
+    # differ from pts in the last bit, which moves a mixed-form gradient)
+    _, grad = fu.fstatnet_grad((u.detach() * w).numpy())
     assert torch.allclose(u.grad, torch.from_numpy(grad) * w, rtol=1e-12, atol=0)
     # the directional derivative along the gradient matches a central
     # difference of F (curvature cancels; tolerance covers the FP32 noise of F)
@@ -193,6 +203,11 @@ def test_ascent_reaches_simplex_maximum(form, fu_case, gpu_ok):
     F1 = -out[:, 5]
     assert np.all(F1 >= F0)
     Fmax = max(-a["out"][5] for a in g["amoeba"])
-    # every start lies within 0.5 widths of the injection: all reach its peak
-    assert np.all(F1 >= Fmax * (1 - 1e-3)), (F1, Fmax)
-    assert np.all(it > 0)
+    # the best start reaches the peak the reference simplex found
+    assert F1.max() >= Fmax * (1 - 1e-3), (F1, Fmax)
+    if fu_case[5].get("unimodal"):
+        # no other maximum within 0.5 widths of the injection: every start
+        # climbs (an accepted step counts one iteration) and reaches its peak;
+        # where local maxima lie that close, a start may already sit on one
+        assert np.all(it > 0)
+        assert np.all(F1 >= Fmax * (1 - 1e-3)), (F1, Fmax)

@@ -11,11 +11,11 @@ from cases import FOLLOWUP_CASES
 from helpers import golden
 
 
-@pytest.fixture(scope="module")
-def fu(tmp_path_factory):
+@pytest.fixture(scope="module", params=[c["name"] for c in FOLLOWUP_CASES])
+def fu(tmp_path_factory, request):
     from polgraw_gb300.lib import Host
     from pyoracle import FollowupOracle
-    case = FOLLOWUP_CASES[0]
+    case = [c for c in FOLLOWUP_CASES if c["name"] == request.param][0]
     g = golden(case["name"])
     tmp = tmp_path_factory.mktemp("fu")
     data = tmp / "data"
