@@ -31,7 +31,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = "/root/reference"
+# location of the reference checkout; override with POLGRAW_REFERENCE
+REFERENCE_ROOT = os.environ.get("POLGRAW_REFERENCE", "/root/reference")
 NETWORK = os.path.join(REFERENCE_ROOT, "search", "network")
 
 ORACLE_LIB = os.path.join(BUILD, "liboracle.so")
@@ -205,6 +206,72 @@ def run_ref_gridgen(ephemeris_dir: str, nfft_exp: int, match: float = 0.75) -> t
             raise RuntimeError("gridgen failed:\n" + r.stdout + r.stderr)
     with open(os.path.join(ephemeris_dir, "grid.bin"), "rb") as f:
         return f.read(), r.stdout
+
+
+REF_BINDING = os.path.join(REF_OUT, "gwsearch-ref-gb300")
+BINDING_DIR = os.path.join(HERE, "ref_binding")
+REPO_INCLUDE = os.path.join(HERE, "..", "include")
+
+
+def patch_jobcore(src: str) -> str:
+    """The reference's search/network/src-cpu/jobcore.c with the GB300
+    job_core binding spliced in: ref_binding/file_scope.c after the
+    include of timer.h (jobcore.c:18), and ref_binding/call_site.c in place
+    of the job_core() call of search() (jobcore.c:107-120)."""
+    import re
+    with open(os.path.join(BINDING_DIR, "file_scope.c")) as f:
+        decls = f.read()
+    with open(os.path.join(BINDING_DIR, "call_site.c")) as f:
+        call = f.read()
+    anchor = '#include "timer.h"\n'
+    if src.count(anchor) != 1:
+        raise RuntimeError("jobcore.c: include anchor not found once")
+    out = src.replace(anchor, anchor + decls, 1)
+    pat = re.compile(r"\n[ \t]*status = job_core\(.*?FNum\);[^\n]*\n", re.S)
+    m = pat.search(out)
+    if not m or "search(" not in out[:m.start()]:
+        raise RuntimeError("jobcore.c: the job_core() call of search() not found")
+    return out[:m.start()] + "\n" + call + out[m.end():]
+
+
+def build_ref_binding(lib_dir: str) -> str | None:
+    """The reference search program with job_core() swapped for the GB300
+    library's pa_job_core() (the maintainer's patch of the reference host):
+    a copy of src-cpu/jobcore.c patched by patch_jobcore() under
+    oracle/_ref/binding/ (never committed), compiled with the reference's
+    other sources against its own headers and the FFTW/GSL shims, and
+    linked to libpolgraw_gb300.so in lib_dir.  Returns None where the
+    reference checkout is absent."""
+    if not reference_available():
+        return None
+    sd = os.path.join(NETWORK, "src-cpu")
+    bdir = os.path.join(REF_OUT, "binding")
+    os.makedirs(bdir, exist_ok=True)
+    with open(os.path.join(sd, "jobcore.c")) as f:
+        patched = patch_jobcore(f.read())
+    pj = os.path.join(bdir, "jobcore.c")
+    with open(pj, "w") as f:
+        f.write(patched)
+    srcs = [pj] + [os.path.join(sd, n) for n in ("main.c", "timer.c", "settings.c", "auxi.c", "init.c")]
+    shims = [os.path.join(HERE, "shim", "fftw_shim.c"), os.path.join(HERE, "shim", "gsl_shim.c"),
+             os.path.join(HERE, "fft.c")]
+    cflags = ["-std=gnu11", "-fcommon", "-O2", "-ffp-contract=off", "-fno-builtin", "-DGNUSINCOS",
+              "-DPREFIX=./candidates", "-DCODEVER=reference-gb300", "-I" + os.path.join(HERE, "shim"),
+              "-I" + sd, "-I" + REPO_INCLUDE]
+    objs = []
+    for k, src in enumerate(srcs + shims):
+        o = os.path.join(bdir, "%d_%s" % (k, os.path.basename(src).replace(".c", ".o")))
+        # the patched file compiles with warnings as errors; the reference's own files as they are
+        warn = ["-Wall", "-Werror", "-Wno-unused-variable", "-Wno-unused-but-set-variable",
+                "-Wno-unused-function", "-Wno-unused-result", "-Wno-maybe-uninitialized",
+                "-Wno-format", "-Wno-misleading-indentation", "-Wno-pointer-sign",
+                "-Wno-implicit-function-declaration", "-Wno-unused-label",
+                "-Wno-stringop-overflow", "-Wno-format-overflow"] if k == 0 else ["-w"]
+        _run([_CC] + cflags + warn + ["-c", src, "-o", o])
+        objs.append(o)
+    _run([_CC, "-o", REF_BINDING] + objs + ["-L" + lib_dir, "-lpolgraw_gb300", "-Wl,-rpath," + lib_dir,
+                                             "-lm", "-lpthread"])
+    return REF_BINDING
 
 
 def build_reference() -> dict:

@@ -8,6 +8,10 @@ import name ``polgraw_gb300`` by a path loader (see ``load_package`` in
 * ``lib``   -- ctypes binding of the C-ABI in include/polgraw_gb300.h
 * ``build`` -- nvcc/gcc recipes for libpolgraw_gb300.so and the C host
 * ``synth`` -- synthetic inputs in the reference's on-disk layout
-* ``host``  -- Python mirror of the reference host set-up (settings, data
-               reading, injection, ranges) used by tests and the bench
+* ``workloads`` -- the benchmark's synthetic workloads (network, precision
+               stress, segments, followup, coincidences)
+* ``replicas`` -- reduction of per-GPU replica timings under torchrun
+
+The reference host set-up itself (settings, data reading, injection,
+ranges) is C, in host/pa_host.c; ``lib.Host`` binds it.
 """

@@ -36,7 +36,14 @@ def materialize(case: dict, root: str) -> dict:
                           fftpad=data["fftpad"], M=[], dets=list(data["dets"]),
                           N=synth.nsamples(data["nod"], data["dt"]))
     g = data.get("grid", {})
-    if "gridgen" in g:
+    if data.get("fixture"):
+        # the reference's own input files (testdata_fixture.py)
+        import testdata_fixture
+        ds = synth.Dataset(root=root, ident=1, band=data["band"], dt=data["dt"], nod=data["nod"],
+                           fftpad=data["fftpad"], M=[], dets=list(data["dets"]),
+                           N=synth.nsamples(data["nod"], data["dt"]))
+        ds.files = testdata_fixture.unpack(root)
+    elif "gridgen" in g:
         # a grid.bin made by the reference grid generator from this case's
         # synthetic ephemeris (make_gridgen_grids.py)
         ds = synth.write_dataset(root, ident=1, band=data["band"], dt=data["dt"], nod=data["nod"],

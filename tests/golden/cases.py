@@ -35,6 +35,18 @@ Coverage (reference file:line of the behaviour each case exercises):
                    places the known line of L1 in the band (lines_in_band)
   cfg1_h1          the 1-detector N=86164 workload: 1 sky point (delta 0.3,
                    alpha 1.2) x 64 spindowns, injected f=0.1 fdot=-1e-8 SNR 12
+  ref_testdata_001 the reference's own input fixture testdata/test-gpu-cpu/001
+                   (H1+L1, N=86164, dt=2 s, band 666: real-shaped noise with
+                   42 % / 53 % gaps of exact zeros, a barycentric ephemeris
+                   and a grid with M4, M8, M9, M12, M13 != 0) with the
+                   command line and range file of the reference's sample run
+                   (search/network/src-gpu/runme, src-gpu/range.dat: 15 sky
+                   points x 81 spindowns, -usedet H1L1, default threshold)
+  ref_testdata_001_wide  the same fixture over 35 sky points x 138 spindowns,
+                   the union of the Smin/Smax spindown ranges of those sky
+                   points (jobcore.c:424-439), threshold 35
+  ref_testdata_001_l1  the same fixture, -usedet L1: one detector and that
+                   detector's own grid.bin (init.c:299-301), threshold 50
 """
 import math
 
@@ -103,6 +115,18 @@ CASES = [
          inject=dict(f=0.1, fdot=-1e-8, delta=0.3, alpha=1.2, snr=12.0),
          range=[-32, 31, 1, 1, 1, 1, None, None],
          args=["-threshold", "20"]),
+    dict(name="ref_testdata_001",
+         data=dict(fixture="testdata_001", dets=["H1", "L1"], dt=2.0, nod=2, band=666, fftpad=1),
+         range=[-40, 40, -1, 1, -2, 2, 1, 1],
+         args=["-usedet", "H1L1"]),
+    dict(name="ref_testdata_001_wide",
+         data=dict(fixture="testdata_001", dets=["H1", "L1"], dt=2.0, nod=2, band=666, fftpad=1),
+         range=[-16, 121, -2, 2, -3, 3, 1, 1],
+         args=["-threshold", "35"]),
+    dict(name="ref_testdata_001_l1",
+         data=dict(fixture="testdata_001", dets=["H1", "L1"], dt=2.0, nod=2, band=666, fftpad=1),
+         range=[-40, 40, -1, 1, -2, 2, 1, 1],
+         args=["-usedet", "L1", "-threshold", "50"]),
 ]
 
 

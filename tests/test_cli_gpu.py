@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("name", ["h1_addsig", "h1l1_gaps_veto", "h1_fullgrid", "h1l1v1_addsig",
                                   "h1v1_lines_usedet", "h1l1_label_pm2",
-                                  "h1l1_amp_fpo"])
+                                  "h1l1_amp_fpo", "ref_testdata_001", "ref_testdata_001_l1"])
 @pytest.mark.parametrize("skybatch", ["1", "7", "7g"])
 def test_cli_trigger_files(name, skybatch, tmp_path, lib, gpu_ok):
     """'7g': 7 sky points per batch, each batch captured as a CUDA graph."""
