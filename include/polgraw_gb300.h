@@ -193,10 +193,12 @@ int pa_debug_fstat(pa_ctx *ctx, int pm, int mm, int nn, int ss,
  * (nmax-nmin doubles) are host memory; all device storage is one static
  * 16 MB array in the library, so sizes are limited to N <= 16384,
  * nfft <= 16384, nfftf <= 32768, nifo <= 3 (larger ones return PA_ERR_ARG
- * with the reason in pa_last_error(NULL)).  The first call on a device sets
- * up the array's device address and should come before any stream
- * capture.  Calls share the array: they are serialised on the host, and
- * calls that overlap on the same GPU race. */
+ * with the reason in pa_last_error(NULL)).  The first call on a device --
+ * and the first after that device's context was reset or replaced -- looks
+ * up the array's device address and should come before any stream capture.
+ * Calls share the array: they are serialised on the host (each waits for
+ * its own GPU work, also when it fails), and calls that overlap on the same
+ * GPU race.  The caller's current device is restored on return. */
 int pa_fstat_noalloc(const pa_settings *sett, const pa_detector *det, int nifo,
                      int pm, int mm, int nn, int ss, const pa_opts *opts,
                      int device, double *F);

@@ -1122,13 +1122,19 @@ int pa_debug_fstat(pa_ctx* c, int pm, int mm, int nn, int ss, const pa_opts* o, 
 // Limits: N <= 16384, nfft <= 16384, nfftf <= 32768, nifo <= 3; larger sizes
 // are rejected with PA_ERR_ARG and a message in pa_last_error(NULL).
 // The first call on a device looks up the array's device address
-// (cudaGetSymbolAddress, with that device current); make that first call
-// before any stream capture.  All calls share the array and it keeps the
-// last call's contents: the call clears what must start at zero (the
+// (cudaGetSymbolAddress, with that device current) and caches it with the
+// id of the device's current CUDA context; a later call in another context
+// of that device (after a cudaDeviceReset, or when the application replaced
+// the primary context) looks the address up again instead of using the
+// stale one.  Make the first call on a device, and the first after such a
+// reset, before any stream capture.  All calls share the array and it keeps
+// the last call's contents: the call clears what must start at zero (the
 // prelude's CTA counter and the candidate count) and overwrites the rest.
-// Calls are serialised on the host by a mutex, but calls that overlap on the
-// GPU (e.g. from another process sharing the device through the same
-// library instance) race on the shared array.
+// Calls are serialised on the host by a mutex and every call, also one that
+// fails part-way, waits for its own copies and kernels before it releases
+// the mutex; calls that overlap on the GPU (e.g. from another process
+// sharing the device through the same library instance) race on the shared
+// array.  The caller's current device is restored on return.
 
 namespace {
 
@@ -1140,7 +1146,52 @@ constexpr int kNoAllocMaxDevices = 64;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 std::mutex g_noalloc_mu;
+// per device: the array's device address and the id of the context it was
+// looked up in (0: not looked up)
 void* g_noalloc_dev_ptr[kNoAllocMaxDevices];
+unsigned long long g_noalloc_ctx_id[kNoAllocMaxDevices];
+
+// The id of the calling thread's current CUDA context (cuCtxGetCurrent +
+// cuCtxGetId, reached through the runtime's driver entry points so that the
+// library needs no link to the driver library); 0 when unavailable, in
+// which case every call looks the address up again.
+unsigned long long noalloc_current_ctx_id() {
+  typedef int (*GetCurrent)(void**);
+  typedef int (*GetId)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      get_current = (GetCurrent)f1;
+      get_id = (GetId)f2;
+    }
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0ull;
+  return id;
+}
+
+// On every return after the lock is taken: wait for what the call enqueued
+// (so that the next call cannot start while this one's copies and kernels
+// still write the array) and make the caller's device current again.
+struct NoAllocExit {
+  cudaStream_t st;
+  int prev_dev;
+  bool enqueued = false;
+  ~NoAllocExit() {
+    if (enqueued) cudaStreamSynchronize(st);
+    if (prev_dev >= 0) cudaSetDevice(prev_dev);
+  }
+};
 alignas(64) unsigned char g_noalloc_engine_mem[4096];
 // host staging: the largest twiddle set (tw1 + tw2 + 1024 + L/1024 complex
 // doubles for L <= 2^16) and one real array of N floats
@@ -1291,18 +1342,25 @@ extern "C" int pa_fstat_noalloc(const pa_settings* sett, const pa_detector* det,
                         kNoAllocBytes);
 
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  int prev_dev = -1;
+  if (cudaGetDevice(&prev_dev) != cudaSuccess) prev_dev = -1;
+  const cudaStream_t st = cudaStreamPerThread;
+  NoAllocExit on_exit{st, prev_dev};
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) return noalloc_fail(PA_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
-  if (!g_noalloc_dev_ptr[device]) {
-    // one-time set-up on this device: the device address of the array
+  const unsigned long long ctx_id = noalloc_current_ctx_id();
+  if (!g_noalloc_dev_ptr[device] || ctx_id == 0 || ctx_id != g_noalloc_ctx_id[device]) {
+    // set-up on this device (or in a new context of it): the device address
+    // of the array
     void* ptr = nullptr;
+    g_noalloc_dev_ptr[device] = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || !ptr)
       return noalloc_fail(PA_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
     g_noalloc_dev_ptr[device] = ptr;
+    g_noalloc_ctx_id[device] = ctx_id;
   }
   noalloc_layout((char*)g_noalloc_dev_ptr[device], *sett, nifo, &b, tw, &Fn);
-  const cudaStream_t st = cudaStreamPerThread;
 
   // host-side scalars of the sky point, as job_core computes them
   pa_ctx c;
@@ -1323,6 +1381,7 @@ extern "C" int pa_fstat_noalloc(const pa_settings* sett, const pa_detector* det,
     if (e_ != cudaSuccess) return noalloc_fail(PA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e_)); \
   } while (0)
   const size_t N = sett->N;
+  on_exit.enqueued = true;
   for (int n = 0; n < nifo; n++) {
     NCK(cudaMemcpyAsync((double*)b.xDat + n * N, det[n].xDat, 8 * N, cudaMemcpyHostToDevice, st), "upload");
     NCK(cudaMemcpyAsync((double*)b.DetSSB + n * 3 * N, det[n].DetSSB, 8 * 3 * N, cudaMemcpyHostToDevice, st),
