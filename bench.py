@@ -142,14 +142,33 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def cpu_baseline(host, tasks, nsky_sample: int, nthreads: int, keep=None):
-    """The CPU oracle (all-FP64 C restatement, OpenMP over spindowns) on a
-    bounded sample of the same sky points: templates/s.  With `keep`, the
-    oracle's candidates are appended to it as {(pm,mm,nn,ss,ii): F}."""
+def cpu_calibration() -> dict | None:
+    """The committed same-host calibration of the oracle's timing build
+    against the reference's own OpenMP search build (oracle/calibrate_cpu.py):
+    port_over_reference > 1 means the timed port is faster than the
+    reference build, i.e. the baseline is not understated."""
+    p = os.path.join(ROOT, "oracle", "cpu_calibration.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return {"port_over_reference": d["port_over_reference"], "host": "%s, %s" % (d["host"], d["cpu"]),
+            "threads": d["threads"], "reference_templates_s": d["reference_omp"]["templates_s"],
+            "port_templates_s": d["port_timing_build"]["templates_s"], "sample": d["sample"],
+            "reference_build": d["reference_omp"]["build"]}
+
+
+def cpu_baseline(host, tasks, nsky_sample: int, nthreads: int, keep=None, fast: bool = True):
+    """The CPU oracle (all-FP64 C restatement, OpenMP over spindowns; by
+    default its build with the reference's timing flags) on a bounded sample
+    of the same sky points: templates/s.  `host` is the oracle-side input
+    set-up (oracle_setup.Inputs) or the product host (same interface).  With
+    `keep`, the oracle's candidates are appended to it as
+    {(pm,mm,nn,ss,ii): F}."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from pyoracle import Oracle
     dets, nifo = host.detectors()
-    orc = Oracle(host.settings, dets, nifo, nthreads=nthreads)
+    orc = Oracle(host.settings, dets, nifo, nthreads=nthreads, fast=fast)
     opts, rng = host.opts(), host.range
     s = host.settings
     bins = s.nmax - s.nmin
@@ -568,6 +587,61 @@ def followup_extra(L, steps: int = 3) -> dict:
 _JSON_FD = 1
 
 
+def run_reference(args) -> None:
+    """The reference arm: the CPU implementation of the path (the oracle's
+    build with the reference's timing flags, OpenMP on every host thread) on
+    the same workload and metric, each step a bounded sample of the sky
+    points.  Its inputs are read by the oracle-side set-up
+    (oracle/oracle_setup.py), so this process loads no library of the
+    product; no GPU is used."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_setup
+    tmp = tempfile.mkdtemp(prefix="pa_bench_ref_")
+    make_workload(tmp, args.spindowns)
+    inp = oracle_setup.Inputs(tmp, ident=1, band=666, dt=2.0, nod=2, range_file=os.path.join(tmp, "range.txt"))
+    tasks = sky_tasks(inp, args.sky)
+    s = inp.settings
+    bins = s.nmax - s.nmin
+    nspin = args.spindowns
+    cfg = {"workload": WORKLOAD, "sky_points": len(tasks), "spindowns": nspin, "bins": bins,
+           "nifo": inp.nifo, "N": s.N, "nfftf": s.nfftf, "parallelism": "host CPU, OpenMP"}
+    nth = os.cpu_count() or 1
+    for _ in range(min(1, args.warmup)):
+        cpu_baseline(inp, tasks, 1, nth)
+    t_all = 0.0
+    ntempl = 0
+    for _ in range(args.steps):
+        v, dt, ns = cpu_baseline(inp, tasks, args.cpu_sky, nth)
+        t_all += dt
+        ntempl += ns * nspin * bins
+    value = ntempl / t_all
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
+                             "sample": "%d sky points x %d spindowns per step (CPU oracle, timing build, "
+                                       "OpenMP)" % (min(args.cpu_sky, len(tasks)), nspin),
+                             "calibration": cpu_calibration()},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0, "libraries_loaded": repo_libraries()}
+    emit(line)
+
+
+def repo_libraries() -> list[str]:
+    """Shared libraries of this repository mapped into the process."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                p = line.split()[-1]
+                if p.startswith(ROOT) and ".so" in os.path.basename(p):
+                    out.add(os.path.relpath(p, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
+
+
 def emit(line: dict) -> None:
     """The one JSON result line, on the original standard output."""
     os.write(_JSON_FD, (json.dumps(line) + "\n").encode())
@@ -612,6 +686,10 @@ def main():
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
     from polgraw_gb300 import build as pbuild, lib as L
     pbuild.build()
     if args.workload == "stress":
@@ -642,31 +720,6 @@ def main():
            "nifo": 2, "N": s.N, "nfftf": s.nfftf, "phase": args.phase,
            "l2": "flushed (256 MB write) before each timed step", "parallelism": "replicas" if world > 1 else "1 GPU"}
 
-    if args.impl == "reference":
-        if rank != 0:
-            return
-        nth = os.cpu_count() or 1
-        vals = []
-        for _ in range(args.warmup if args.warmup < 1 else 1):
-            cpu_baseline(host, tasks, 1, nth)
-        t_all = 0.0
-        ntempl = 0
-        for _ in range(args.steps):
-            v, dt, ns = cpu_baseline(host, tasks, args.cpu_sky, nth)
-            vals.append(v)
-            t_all += dt
-            ntempl += ns * nspin * bins
-        value = ntempl / t_all
-        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": cfg,
-                "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
-                                 "sample": "%d sky points x %d spindowns per step (CPU oracle, OpenMP)" %
-                                           (args.cpu_sky, nspin)},
-                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        emit(line)
-        return
 
     # N > 1: one replica of the whole workload per GPU (sky points are
     # independent, nothing is exchanged); the step time is the maximum over
@@ -791,20 +844,21 @@ def main():
             ref = {}
             cv, cdt, cn = cpu_baseline(host, tasks, args.cpu_sky, nth, keep=ref)
             out["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": nth, "kind": "port",
-                                   "sample": "%d sky points x %d spindowns (CPU oracle, OpenMP, %.1f s)" %
-                                             (cn, nspin, cdt)}
+                                   "sample": "%d sky points x %d spindowns (CPU oracle, timing build, OpenMP, "
+                                             "%.1f s)" % (cn, nspin, cdt),
+                                   "calibration": cpu_calibration()}
             # and the serial form on one core (the reference's src-cpu build)
             c1v, c1dt, c1n = cpu_baseline(host, tasks, 1, 1)
             out["cpu_baseline_1core"] = {"value": c1v, "unit": UNIT, "cores": 1, "kind": "port",
-                                         "sample": "1 sky point x %d spindowns (CPU oracle, one thread, %.1f s)" %
-                                                   (nspin, c1dt)}
+                                         "sample": "1 sky point x %d spindowns (CPU oracle, timing build, one "
+                                                   "thread, %.1f s)" % (nspin, c1dt)}
             # relative F-statistic error of the mixed form against the FP64 CPU oracle
             rg, ig, _ = ctx.search_batch(tasks[:cn], opts, rng)
             got = {tuple(int(x[f]) for f in ("pm", "mm", "nn", "ss", "ii")): r[4] * r[4] / 2 + 2
                    for x, r in zip(ig, rg)}
             common = [k for k in ref if k in got]
             edge = lambda F: abs(F - opts.trl) <= 1e-4 * opts.trl  # noqa: E731
-            out["vs_oracle"] = {"sky_points": cn, "candidates": len(ref),
+            out["vs_oracle"] = {"sky_points": cn, "candidates": len(ref), "oracle": "timing build",
                                 "fstat_rel_err_max": max([abs(got[k] - ref[k]) / ref[k] for k in common],
                                                          default=0.0),
                                 "index_mismatches": sum(1 for k in ref if k not in got and not edge(ref[k])) +

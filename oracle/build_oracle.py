@@ -69,6 +69,27 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_LIB
 
 
+ORACLE_FAST_LIB = os.path.join(BUILD, "liboracle_fast.so")
+
+
+def build_oracle_fast(force: bool = False) -> str:
+    """The same oracle sources with the reference's timing flags
+    (search/network/src-openmp/Makefile:13-18: -O3 -funroll-loops
+    -ffast-math with OpenMP; its -march=haswell/-mavx2/-mfma are x86 only
+    and left out so that the build runs on both host architectures): the
+    timed CPU baseline of bench.py, never a parity reference."""
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = [os.path.join(HERE, f) for f in ("oracle.c", "fft.c", "oracle_coinc.c", "shim/gsl_shim.c")]
+    deps = srcs + [os.path.join(HERE, f) for f in ("oracle.h", "fft.h", "shim/gsl/pa_gsl_shim.h")] + [
+        os.path.join(HERE, "..", "include", "polgraw_gb300.h")]
+    if force or _newer(ORACLE_FAST_LIB, deps):
+        tmp = ORACLE_FAST_LIB + ".tmp%d" % os.getpid()
+        _run([_CC, "-std=gnu11", "-O3", "-funroll-loops", "-ffast-math", "-fPIC", "-shared", "-fopenmp",
+              "-Wall", "-Wno-unused", "-I" + os.path.join(HERE, "shim"), "-o", tmp] + srcs + ["-lm"])
+        os.replace(tmp, ORACLE_FAST_LIB)
+    return ORACLE_FAST_LIB
+
+
 def reference_available() -> bool:
     return os.path.isdir(os.path.join(NETWORK, "src-cpu"))
 
@@ -298,4 +319,5 @@ def build_reference() -> dict:
 
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
+    print(build_oracle_fast(force="--force" in sys.argv))
     print(build_reference())

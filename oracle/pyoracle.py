@@ -17,13 +17,18 @@ sys.path.insert(0, HERE)
 import build_oracle  # noqa: E402
 
 _lib = None
+_lib_fast = None
 
 
-def load():
-    global _lib
-    if _lib is not None:
+def load(fast: bool = False):
+    """The parity oracle (liboracle.so), or with fast=True its build with the
+    reference's timing flags (liboracle_fast.so, the timed CPU baseline)."""
+    global _lib, _lib_fast
+    if fast and _lib_fast is not None:
+        return _lib_fast
+    if not fast and _lib is not None:
         return _lib
-    path = build_oracle.build_oracle()
+    path = build_oracle.build_oracle_fast() if fast else build_oracle.build_oracle()
     lib = C.CDLL(path)
     lib.ora_create.restype = C.c_void_p
     lib.ora_create.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
@@ -37,7 +42,10 @@ def load():
     lib.ora_search_settings.argtypes = [C.c_void_p]
     lib.ora_search_settings.restype = None
     lib.ora_spindown_range.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, P(C.c_int), P(C.c_int)]
-    _lib = lib
+    if fast:
+        _lib_fast = lib
+    else:
+        _lib = lib
     return lib
 
 
@@ -45,8 +53,8 @@ class Oracle:
     """All-FP64 CPU restatement of job_core() over the same pa_settings /
     pa_detector inputs as the GPU context."""
 
-    def __init__(self, settings, dets, nifo: int, nthreads: int = 0):
-        self.lib = load()
+    def __init__(self, settings, dets, nifo: int, nthreads: int = 0, fast: bool = False):
+        self.lib = load(fast)
         self.settings = settings
         self.nifo = nifo
         self.o = self.lib.ora_create(C.addressof(settings), C.cast(dets, C.c_void_p), nifo, nthreads)

@@ -1,7 +1,9 @@
 """bench.py's reference arm on the CPU: one bounded step of the CPU oracle on
 the H1+L1 N=86164 workload (1 sky point x 8 spindowns) prints exactly one JSON
 line carrying the bench contract's keys, with the CPU baseline and an e2e
-figure that moves no bytes to or from a device."""
+figure that moves no bytes to or from a device, having loaded no library of
+the product (only the oracle's), and reports the committed
+same-host calibration against the reference's own OpenMP build."""
 import json
 import os
 import subprocess
@@ -30,3 +32,9 @@ def test_reference_arm_prints_one_contract_line(lib):
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    # the CPU arm reads its inputs with the oracle's own set-up: no library
+    # of the product is loaded, only the oracle's timing build
+    libs = d["libraries_loaded"]
+    assert "oracle/_build/liboracle_fast.so" in libs and all(x.startswith("oracle/") for x in libs), libs
+    cal = cb["calibration"]
+    assert cal is not None and cal["port_over_reference"] > 0
