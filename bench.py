@@ -587,6 +587,75 @@ def followup_extra(L, steps: int = 3) -> dict:
 _JSON_FD = 1
 
 
+def run_cta_trace(ctx, tasks, opts, rng, cfg, templates_per_sky) -> dict:
+    """One step with the per-CTA trace on (diagnostic build): how much of the
+    step the GPU runs no CTA at all (gaps between kernels and launch
+    latency), how busy the SMs are (partial waves, tails), and the CTA time
+    of each kernel kind.  All times from %globaltimer of the CTAs' first and
+    last instruction of thread 0."""
+    import torch
+    REC = np.dtype([("t0", "<u8"), ("t1", "<u8"), ("c0", "<u8"), ("c1", "<u8"), ("kind", "<u4"),
+                    ("smid", "<u4"), ("p0", "<u4"), ("p1", "<u4")])
+    cap = 1 << 23
+    buf = torch.zeros(cap * REC.itemsize, dtype=torch.uint8, device="cuda")
+    ctx.set_cta_trace(buf.data_ptr(), cap)
+    l2_flush()
+    ctx.search_batch(tasks, opts, rng)
+    step_ms = ctx.last_call_ms()
+    n = ctx.cta_trace_count()
+    ctx.set_cta_trace(0, 0)
+    r = np.frombuffer(buf[:min(n, cap) * REC.itemsize].cpu().numpy().tobytes(), dtype=REC)
+    r = r[r["t1"] > 0]
+    t0 = r["t0"].astype(np.int64)
+    t1 = r["t1"].astype(np.int64)
+    base = t0.min()
+    t0 -= base
+    t1 -= base
+    span = int(t1.max())
+
+    def union(a, b):
+        o = np.argsort(a, kind="stable")
+        a, b = a[o], b[o]
+        busy, cur_a, cur_b, gaps = 0, a[0], b[0], []
+        for x, y in zip(a[1:], b[1:]):
+            if x > cur_b:
+                busy += cur_b - cur_a
+                gaps.append(x - cur_b)
+                cur_a, cur_b = x, y
+            elif y > cur_b:
+                cur_b = y
+        busy += cur_b - cur_a
+        return int(busy), np.array(gaps, dtype=np.int64)
+
+    busy, gaps = union(t0, t1)
+    nsm = int(r["smid"].max()) + 1
+    sm_busy = []
+    for sm in range(nsm):
+        m = r["smid"] == sm
+        sm_busy.append(union(t0[m], t1[m])[0] if m.any() else 0)
+    names = {k: L_kind for k, L_kind in enumerate(
+        ["prelude_mod", "fft_fwd_a", "fft_fwd_b", "fft_inv_a", "fft_inv_b", "spline_fwd", "spline_bwd",
+         "splint", "spindown_pass_a", "spindown_pass_b_fstat", "threshold"])}
+    kinds = {}
+    cta_ns = (t1 - t0).astype(np.float64)
+    for k in np.unique(r["kind"]):
+        m = r["kind"] == k
+        kinds[names.get(int(k), str(int(k)))] = {"ctas": int(m.sum()), "cta_ms": float(cta_ns[m].sum() / 1e6),
+                                                "mean_cta_us": float(cta_ns[m].mean() / 1e3)}
+    ut = np.unique(np.concatenate([t0, t1]))
+    return {"cta_trace": {
+        "workload": cfg["workload"], "sky_points": len(tasks), "step_ms_events": step_ms,
+        "span_ms": span / 1e6, "ctas": int(len(r)), "dropped": int(max(0, n - cap)),
+        "gpu_idle_frac": 1.0 - busy / span, "gaps": int(len(gaps)),
+        "gaps_over_1us": int((gaps > 1000).sum()), "gap_ms_total": float(gaps.sum() / 1e6),
+        "gap_us_median": float(np.median(gaps) / 1e3) if len(gaps) else 0.0,
+        "sm_busy_frac_mean": float(np.mean(sm_busy) / span), "sm_busy_frac_min": float(np.min(sm_busy) / span),
+        "cta_slots_mean": float(cta_ns.sum() / (nsm * span)), "sms": nsm,
+        "timer_resolution_ns": int(np.diff(ut).min()) if len(ut) > 1 else 0,
+        "templates_per_s_traced": len(tasks) * templates_per_sky / (step_ms / 1e3),
+        "kinds": kinds}}
+
+
 def run_reference(args) -> None:
     """The reference arm: the CPU implementation of the path (the oracle's
     build with the reference's timing flags, OpenMP on every host thread) on
@@ -682,6 +751,10 @@ def main():
     ap.add_argument("--autotune", type=int, default=1,
                     help="tune the spindown schedule (pa_autotune) on 8 sky points before timing (1) or not (0)")
     ap.add_argument("--cpu-candidates", type=int, default=4, help="followup: CPU simplex sample")
+    ap.add_argument("--cta-trace", type=int, default=0,
+                    help="network workload: instead of the timed steps, one step of the diagnostic build "
+                         "with the per-CTA trace on; prints the launch-structure summary (idle fraction, "
+                         "gaps, SM busy fraction, CTA time per kernel)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -692,6 +765,9 @@ def main():
         return
     from polgraw_gb300 import build as pbuild, lib as L
     pbuild.build()
+    if args.cta_trace:
+        # the diagnostic build with the per-CTA trace compiled in
+        L.load(pbuild.build(trace=True))
     if args.workload == "stress":
         if rank == 0:
             run_stress(args, L)
@@ -748,6 +824,12 @@ def main():
     lanes = ctx.lanes()
     for _ in range(args.warmup):
         ctx.search_batch(tasks, opts, rng)
+    if args.cta_trace:
+        if rank == 0:
+            emit(run_cta_trace(ctx, tasks, opts, rng, cfg, nspin * bins))
+        ctx.close()
+        replicas.shutdown()
+        return
     launches0 = ctx.launches()
     replicas.barrier()
     clocks = ClockSampler(device)

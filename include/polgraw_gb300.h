@@ -226,6 +226,20 @@ void pa_profile_reset(pa_ctx *ctx);
 int pa_profile_get(const pa_ctx *ctx, int kind, const char **name, double *total_ms,
                    long long *launches, long long *items);
 
+/* Per-CTA trace of the context's kernels (a diagnostic of the launch
+ * structure: gaps between kernels, partial waves).  dev_buf: device memory
+ * for cap records of 48 bytes, {start %globaltimer ns, end %globaltimer ns,
+ * start clock64, end clock64 (uint64 each), kernel kind, SM id, 2 x pad
+ * (uint32 each)}, one per CTA, appended in completion order by the CTA's
+ * thread 0; NULL switches the trace off (the default).  Setting it resets
+ * the count.  pa_cta_trace_count: records written since (may exceed cap;
+ * the excess is dropped).  Kernel kinds are those of pa_profile_get.
+ * Only the diagnostic build of the library (compiled with -DPA_CTA_TRACE)
+ * records the trace; the product build returns PA_ERR_CUDA with "operation
+ * not supported". */
+int pa_set_cta_trace(pa_ctx *ctx, void *dev_buf, unsigned int cap);
+int pa_cta_trace_count(pa_ctx *ctx, unsigned int *n);
+
 /* ------------------------------------------------------------------------
  * Launch schedule, CUDA graphs and the multi-segment front-end.  No
  * counterpart in the reference (one process per segment and sky range,

@@ -55,32 +55,45 @@ def _stale(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+TRACE_BUILD = os.path.join(HERE, "_build_trace")
+TRACE_LIB = os.path.join(TRACE_BUILD, "libpolgraw_gb300.so")
+
+
+def build(force: bool = False, verbose: bool = False, trace: bool = False) -> str:
+    """Builds the library (and the programs) into _build/.  trace=True builds
+    the diagnostic variant with the per-CTA trace compiled in
+    (-DPA_CTA_TRACE) into _build_trace/ instead (library only); it is used
+    only by the benchmark's --cta-trace measurement."""
+    out_dir = TRACE_BUILD if trace else BUILD
+    lib_path = TRACE_LIB if trace else LIB
+    os.makedirs(out_dir, exist_ok=True)
     nvcc = _nvcc()
+    nvcc_flags = NVCC_FLAGS + (["-DPA_CTA_TRACE"] if trace else [])
     headers = [os.path.join(HERE, h) for h in HEADERS] + [
         os.path.join(INCLUDE, "polgraw_gb300.h"), os.path.join(INCLUDE, "polgraw_gb300_host.h")]
     jobs = []
     objs = []
     for s in CU_SOURCES:
         src = os.path.join(HERE, s)
-        obj = os.path.join(BUILD, os.path.basename(s) + ".o")
+        obj = os.path.join(out_dir, os.path.basename(s) + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nvcc] + nvcc_flags + ["-c", src, "-o", obj])
     for s in C_SOURCES:
         src = os.path.join(HERE, s)
-        obj = os.path.join(BUILD, os.path.basename(s) + ".o")
+        obj = os.path.join(out_dir, os.path.basename(s) + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append(["gcc"] + CC_FLAGS + ["-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
-    if force or _stale(LIB, objs):
-        tmp = LIB + ".tmp%d" % os.getpid()
+    if force or _stale(lib_path, objs):
+        tmp = lib_path + ".tmp%d" % os.getpid()
         _run([nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs + ["-lpthread"])
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib_path)
+    if trace:
+        return lib_path
     for exe, main in ((EXE, "gwsearch_gb300.c"), (COINC_EXE, "coincidences_gb300.c")):
         main_src = os.path.join(HERE, "host", main)
         if force or _stale(exe, [LIB, main_src]):

@@ -496,6 +496,22 @@ int pa_set_profiling(pa_ctx* c, int on) {
   return PA_OK;
 }
 
+int pa_set_cta_trace(pa_ctx* c, void* buf, unsigned int cap) {
+  if (!c || !c->eng) return PA_ERR_ARG;
+  CK(cudaSetDevice(c->dev), "cudaSetDevice");
+  CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+  CK(c->eng->set_trace(buf, cap), "set trace");
+  return PA_OK;
+}
+
+int pa_cta_trace_count(pa_ctx* c, unsigned int* n) {
+  if (!c || !c->eng || !n) return PA_ERR_ARG;
+  CK(cudaSetDevice(c->dev), "cudaSetDevice");
+  CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+  CK(c->eng->trace_count(n), "trace count");
+  return PA_OK;
+}
+
 void pa_profile_reset(pa_ctx* c) {
   if (!c) return;
   for (int k = 0; k < pa::KK_COUNT; k++) {

@@ -95,6 +95,7 @@ __global__ void __launch_bounds__(256)
                   double* __restrict__ part, double* __restrict__ sums, R* __restrict__ sums_r,
                   unsigned int* __restrict__ counter) {
   typedef typename CT<R>::T T;
+  CtaTrace trace_(KK_PRELUDE_MOD);
   const int d = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   R a2r = 0, b2r = 0;
@@ -258,6 +259,7 @@ __global__ void __launch_bounds__(256)
 
 template <typename R> struct PlainLoader {
   typedef typename CT<R>::T T;
+  static constexpr int kTraceKind = KK_FFT_FWD_A;
   const T* in;   // [batch][2][ld]
   int len, ld;
   __device__ __forceinline__ void prologue(int, char*) const {}
@@ -283,6 +285,7 @@ template <typename R> struct PlainLoader {
 // zero gap.  This loader feeds that transform; InterpStore interleaves.
 template <typename R> struct HalfShiftLoader {
   typedef typename CT<R>::T T;
+  static constexpr int kTraceKind = KK_FFT_INV_A;
   const T* spec;    // [batch][2][nfft]
   const T* twlo;    // e^{+2 pi i m/Ninterp}, m < 1024
   const T* twhi;    // e^{+2 pi i 1024 m/Ninterp}
@@ -312,6 +315,7 @@ __device__ __forceinline__ uint64_t mul64x32(uint64_t a, unsigned b) {
 //   x_{a,b}[n] = sum_d xm_{a,b,d}[n] exp(-i (het1 n + s1 tmp1_d[n]))  (n < N)
 template <typename R, int PM> struct SpinLoader {
   typedef typename CT<R>::T T;
+  static constexpr int kTraceKind = KK_SPIN_A;
   const T* xm;       // [nifo][2][N]
   const void* ph0;   // FP64 form: tmp1 [nifo][N]; FP32 forms: unused
   int N, nifo, ss0, ss_base, s0_flag;
@@ -492,6 +496,7 @@ __global__ void __launch_bounds__(512, 2)
                const float2* __restrict__ twhi, float2* __restrict__ ybuf) {
   constexpr int LOGL1 = 8, LOGL2 = LOGL - LOGL1, ZC = 16 * 32 + 2;
   constexpr int Lmask = (1 << LOGL) - 1;
+  CtaTrace trace_(KK_SPIN_A);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* z = reinterpret_cast<float2*>(smem_raw);
   float2* tws = z + 16 * ZC;
@@ -553,6 +558,7 @@ template <int PM> struct IsSpinF32<SpinLoader<float, PM>> {
 // Complex output with a scale factor (resampling FFTs).
 template <typename R> struct CStore {
   typedef typename CT<R>::T T;
+  static constexpr int kTraceKind = KK_FFT_FWD_B;
   T* out;   // [batch][2][ldo]
   int ldo;
   R scale;
@@ -567,6 +573,7 @@ template <typename R> struct CStore {
 // F-statistic epilogue: F[k] = |Xa[k]|^2 / aa + |Xb[k]|^2 / bb, k in [nmin, nmax)
 template <typename R> struct FstatStore {
   typedef typename CT<R>::T T;
+  static constexpr int kTraceKind = KK_SPIN_B;
   R* F;             // [batch][bins]
   const R* inv;     // 1/aa, 1/bb in the working precision
   int nmin, nmax, bins;
@@ -585,6 +592,7 @@ template <typename R> struct FstatStore {
 // 16-byte pair per (array, m) into yint [batch][2][Ninterp].
 template <typename R> struct InterpStore {
   typedef typename CT<R>::T T;
+  static constexpr int kTraceKind = KK_FFT_INV_B;
   T* yint;
   const T* xin;     // [batch][2][N]
   int N, Ninterp;
@@ -703,6 +711,7 @@ __global__ void __launch_bounds__(kSplineThreads)
     k_spline_fwd(const typename CT<R>::T* __restrict__ y, int ldy, double2* __restrict__ u, int n, int nseg,
                  const double* __restrict__ invp) {
   typedef typename CT<R>::T T;
+  CtaTrace trace_(KK_SPLINE_FWD);
   extern __shared__ __align__(16) unsigned char sm_raw[];
   double2* us = reinterpret_cast<double2*>(sm_raw);                 // spad_len<R>(kSplineSeg)
   T* ys = reinterpret_cast<T*>(us + spad_len<R>(kSplineSeg));          // spad_len<R>(kSplineSeg + SplineCfg<R>::warm + 2)
@@ -788,6 +797,7 @@ __global__ void __launch_bounds__(kSplineThreads)
     k_spline_bwd(const double2* __restrict__ u, typename CT<R>::T* __restrict__ y2, int n, int nseg,
                  const double* __restrict__ ptab) {
   typedef typename CT<R>::T T;
+  CtaTrace trace_(KK_SPLINE_BWD);
   extern __shared__ __align__(16) unsigned char sm_raw[];
   double2* us = reinterpret_cast<double2*>(sm_raw);                     // spad_len<R>(kSplineSeg + SplineCfg<R>::warm)
   T* ys = reinterpret_cast<T*>(us + spad_len<R>(kSplineSeg + SplineCfg<R>::warm));  // spad_len<R>(kSplineSeg)
@@ -850,6 +860,7 @@ __global__ void __launch_bounds__(256)
              const double* __restrict__ shftf, const DetConst* __restrict__ dc, int N,
              typename CT<R>::T* __restrict__ xm) {
   typedef typename CT<R>::T T;
+  CtaTrace trace_(KK_SPLINT);
   const int d = blockIdx.y;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
@@ -936,6 +947,7 @@ __global__ void __launch_bounds__(256)
                  DevCand* __restrict__ cand, int* __restrict__ ncand, int cap, R* __restrict__ Fdbg) {
   __shared__ R sv[4096 + 1];
   __shared__ R red[8];
+  CtaTrace trace_(KK_THRESHOLD);
   const int c = blockIdx.x, sidx = blockIdx.y;
   const int nchunk = (bins + 4095) >> 12;
   const R* f = F + (size_t)sidx * bins;
@@ -1177,6 +1189,20 @@ template <typename R, int PM> class EngineT : public Engine {
   long long launches() const override { return launches_; }
   size_t real_size() const override { return sizeof(R); }
   void set_split(int split) override { split_ = (gm_.logL & 1) ? split : 0; }
+#ifdef PA_CTA_TRACE
+  cudaError_t set_trace(void* buf, unsigned int cap) override {
+    CtaTraceRec* p = static_cast<CtaTraceRec*>(buf);
+    const unsigned int zero = 0, c = buf ? cap : 0u;
+    cudaError_t e = cudaMemcpyToSymbol(c_trace_buf, &p, sizeof(p));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_trace_cap, &c, sizeof(c));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_trace_n, &zero, sizeof(zero));
+    return e;
+  }
+  cudaError_t trace_count(unsigned int* n) override { return cudaMemcpyFromSymbol(n, g_trace_n, sizeof(*n)); }
+#else
+  cudaError_t set_trace(void*, unsigned int) override { return cudaErrorNotSupported; }
+  cudaError_t trace_count(unsigned int*) override { return cudaErrorNotSupported; }
+#endif
   int split() const override { return split_; }
 
   cudaError_t prelude(const SkyArgs& sky, int slot, cudaStream_t st) override {

@@ -132,6 +132,12 @@ class Engine {
   // odd m only; ignored for even m).
   virtual void set_split(int split) = 0;
   virtual int split() const = 0;
+  // Per-CTA trace of this engine's kernels into buf (cap records of 48
+  // bytes: start/end %globaltimer, start/end clock64, kernel kind, SM id);
+  // buf == nullptr switches it off.  trace_count: records written so far
+  // (may exceed cap; the excess is dropped).
+  virtual cudaError_t set_trace(void* buf, unsigned int cap) = 0;
+  virtual cudaError_t trace_count(unsigned int* n) = 0;
 };
 
 // Factories (defined in the per-precision translation units).

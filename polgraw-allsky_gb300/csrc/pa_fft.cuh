@@ -327,6 +327,65 @@ template <typename R, int LOGL, int SPLIT = 0> struct FftShape {
   static_assert(C <= L2 && RR <= L1, "transform too short for the tile");
 };
 
+// Optional per-CTA trace, a diagnostic of the launch structure (gaps
+// between kernels, partial waves): when a trace buffer is set
+// (Engine::set_trace), thread 0 of every CTA of the engine's kernels
+// fills one record {%globaltimer at start and end, clock64 at start and
+// end, kernel kind, SM id}, in the order the CTAs start.  The variables are
+// per translation unit (static): each engine sets those of its own unit.
+struct CtaTraceRec {
+  unsigned long long t0, t1, c0, c1;
+  unsigned int kind, smid, pad0, pad1;
+};
+#ifdef PA_CTA_TRACE
+static __constant__ CtaTraceRec* c_trace_buf;
+static __constant__ unsigned int c_trace_cap;
+static __device__ unsigned int g_trace_n;
+#endif
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// The record's slot is taken when the CTA starts, so that only its index
+// stays live in a register through the kernel.  Even that register can
+// make a 64-register kernel spill, so the trace exists only in the
+// diagnostic build (-DPA_CTA_TRACE, polgraw-allsky_gb300/build.py
+// build(trace=True)); in the product build CtaTrace is empty.
+#ifdef PA_CTA_TRACE
+struct CtaTrace {
+  unsigned int slot = 0xffffffffu;
+  __device__ __forceinline__ explicit CtaTrace(int kind) {
+    if (c_trace_buf && threadIdx.x == 0) {
+      const unsigned long long t0 = global_ns(), c0 = clock64();
+      const unsigned int i = atomicAdd(&g_trace_n, 1u);
+      if (i < c_trace_cap) {
+        unsigned int smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        c_trace_buf[i].t0 = t0;
+        c_trace_buf[i].c0 = c0;
+        c_trace_buf[i].kind = (unsigned int)kind;
+        c_trace_buf[i].smid = smid;
+        slot = i;
+      }
+    }
+  }
+  __device__ __forceinline__ ~CtaTrace() {
+    if (slot != 0xffffffffu) {
+      const unsigned long long c1 = clock64(), t1 = global_ns();
+      c_trace_buf[slot].c1 = c1;
+      c_trace_buf[slot].t1 = t1;
+    }
+  }
+};
+#else
+struct CtaTrace {
+  __device__ __forceinline__ explicit CtaTrace(int) {}
+};
+#endif
+
 // Pass A: column FFTs of length L1 over C columns x 2 arrays of one batch
 // item (blockIdx.y).  The first radix stage takes its inputs from the
 // loader in registers; the last stage (lanes along k1) applies the
@@ -341,6 +400,7 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
   typedef typename CT<R>::T T;
   typedef FftShape<R, LOGL, SPLIT> G;
   constexpr int E = G::E, NT = G::NT, P = G::PA;
+  CtaTrace trace_(Loader::kTraceKind);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s = reinterpret_cast<T*>(smem_raw);
   T* tws = s + G::L1 * P;
@@ -386,6 +446,7 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
   typedef typename CT<R>::T T;
   typedef FftShape<R, LOGL, SPLIT> G;
   constexpr int E = G::E, NT = G::NT, P = G::PB;
+  CtaTrace trace_(Storer::kTraceKind);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s = reinterpret_cast<T*>(smem_raw);
   T* tws = s + G::L2 * P;

@@ -27,6 +27,7 @@ EXPORTS = [
     "pa_version", "pa_device_count", "pa_create", "pa_set_data", "pa_destroy", "pa_last_error",
     "pa_job_core", "pa_search_batch", "pa_debug_prelude", "pa_debug_fstat", "pa_kernel_launches",
     "pa_last_call_ms", "pa_set_profiling", "pa_profile_reset", "pa_profile_get", "pa_fstat_noalloc",
+    "pa_set_cta_trace", "pa_cta_trace_count",
     "pa_host_create", "pa_host_setup", "pa_host_search", "pa_host_main", "pa_host_destroy",
     "pa_host_settings", "pa_host_detectors", "pa_host_range", "pa_host_core_opts",
     "pa_host_config", "pa_host_detector_name",
@@ -128,6 +129,8 @@ def load(path: str | None = None) -> C.CDLL:
     lib.pa_last_call_ms.restype = C.c_double
     lib.pa_last_call_ms.argtypes = [C.c_void_p]
     lib.pa_set_profiling.argtypes = [C.c_void_p, C.c_int]
+    lib.pa_set_cta_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_uint]
+    lib.pa_cta_trace_count.argtypes = [C.c_void_p, P(C.c_uint)]
     lib.pa_profile_reset.argtypes = [C.c_void_p]
     lib.pa_profile_reset.restype = None
     lib.pa_profile_get.argtypes = [C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_longlong),
@@ -413,6 +416,19 @@ class Context:
 
     def profile_reset(self):
         self.lib.pa_profile_reset(self.ctx)
+
+    def set_cta_trace(self, dev_ptr: int, cap: int):
+        """Per-CTA trace into device memory at dev_ptr (cap 48-byte records);
+        dev_ptr 0 switches it off."""
+        rc = self.lib.pa_set_cta_trace(self.ctx, C.c_void_p(dev_ptr or None), cap)
+        if rc != PA_OK:
+            raise SearchError("pa_set_cta_trace failed: %s" % self.error())
+
+    def cta_trace_count(self) -> int:
+        n = C.c_uint(0)
+        if self.lib.pa_cta_trace_count(self.ctx, C.byref(n)) != PA_OK:
+            raise SearchError("pa_cta_trace_count failed: %s" % self.error())
+        return n.value
 
     def profile(self) -> dict:
         """{kernel name: (total_ms, launches, items)}"""

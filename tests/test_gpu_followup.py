@@ -192,9 +192,50 @@ def test_simplex_matches_reference(form, fu_case, gpu_ok):
     assert np.array_equal(p1[0], pts[1]) and n1[0] == nev[1]
 
 
+def _oracle_ascent(orc, start, w, step0, min_step, max_iter):
+    """The ascent of pa_followup_ascent (BFGS on -F in peak-width units
+    u = theta / w, backtracking line search with the sufficient-increase
+    factor 1e-4, inverse-Hessian update when y.s > 0, stop when the step
+    falls below min_step, the slope is not positive, or after max_iter
+    accepted steps) restated in FP64 on the oracle's F and gradient.
+    Returns (end point, F there, accepted steps)."""
+    theta = np.array(start, dtype=np.float64)
+    F, g = orc.fstatnet_grad(theta)
+    gu = w * g
+    nrm = np.linalg.norm(gu)
+    if not nrm > 0:
+        return theta, F, 0
+    H = np.eye(4) * (step0 / nrm)
+    t, iters = 1.0, 0
+    while iters < max_iter:
+        p = H @ gu
+        slope = float(p @ gu)
+        if not slope > 0 or t * np.linalg.norm(p) < min_step:
+            break
+        trial = theta + w * t * p
+        Ft = -orc.fstatnet(trial)[5]
+        if Ft >= F + 1e-4 * t * slope and Ft > F:
+            s = t * p
+            gold = gu
+            theta, F = trial, Ft
+            _, g = orc.fstatnet_grad(theta)
+            gu = w * g
+            y = gold - gu
+            ys = float(y @ s)
+            if ys > 0:
+                r = 1.0 / ys
+                Hy = H @ y
+                H = H - r * (np.outer(s, Hy) + np.outer(Hy, s)) + (r * r * float(y @ Hy) + r) * np.outer(s, s)
+            t = 1.0
+            iters += 1
+        else:
+            t *= 0.5
+    return theta, F, iters
+
+
 @pytest.mark.parametrize("form", list(FORMS))
 def test_ascent_reaches_simplex_maximum(form, fu_case, gpu_ok):
-    g = fu_case[3]
+    g, orc = fu_case[3], fu_case[4]
     fu = _fu(fu_case, form)
     w = np.array(g["widths"])
     starts = np.array(g["points"][1:])
@@ -207,7 +248,42 @@ def test_ascent_reaches_simplex_maximum(form, fu_case, gpu_ok):
     assert F1.max() >= Fmax * (1 - 1e-3), (F1, Fmax)
     if fu_case[5].get("unimodal"):
         # no other maximum within 0.5 widths of the injection: every start
-        # climbs (an accepted step counts one iteration) and reaches its peak;
-        # where local maxima lie that close, a start may already sit on one
-        assert np.all(it > 0)
+        # reaches its peak
         assert np.all(F1 >= Fmax * (1 - 1e-3)), (F1, Fmax)
+    # every path, not only the best: the same ascent in FP64 on the oracle
+    # from each start.  Every start off a stationary point takes at least one
+    # step; every end point is a stationary point of the oracle's F, not
+    # below the start; in the FP64 form each path ends where the oracle's
+    # does (F and point).  A mixed-precision path may part from the FP64 one
+    # where several stationary points lie within half a width (fu_h1l1_dt2:
+    # maxima near 151.6 and 152.1, and flat saddles between them, where the
+    # rounding noise of the FP32 gradient can end the ascent): it must then
+    # still end on a stationary point of the oracle's F within 1 % of the
+    # oracle path's F.  On fu_h1l1v1, whose F has no other stationary point
+    # within half a width of the peak, no path may part.
+    ftol = FORMS[form][1]
+    worst_f = worst_p = worst_g = 0.0
+    parted = []
+    for k, st in enumerate(starts):
+        Fs, gs = orc.fstatnet_grad(st)
+        if np.abs(w * gs).max() > 1e-2 * Fs:
+            assert it[k] > 0, (k, np.abs(w * gs).max() / Fs)
+        pe, Fe, ie = _oracle_ascent(orc, st, w, 0.25, 1e-4, 200)
+        Fg, gg = orc.fstatnet_grad(pts[k])
+        assert Fg >= Fs * (1 - ftol), (k, Fg, Fs)
+        worst_g = max(worst_g, float(np.abs(w * gg).max() / Fg))
+        assert np.abs(w * gg).max() <= 2e-3 * Fg, (k, np.abs(w * gg).max() / Fg)
+        if abs(Fg - Fe) > 1e-3 * Fe:
+            assert form != "fp64", (k, Fg, Fe)
+            assert abs(Fg - Fe) <= 1e-2 * Fe, (k, Fg, Fe)
+            parted.append((k, round(Fg, 3), round(Fe, 3)))
+            continue
+        worst_f = max(worst_f, abs(Fg - Fe) / Fe)
+        worst_p = max(worst_p, float(np.abs((pts[k] - pe) / w).max()))
+        if form == "fp64":
+            assert np.abs((pts[k] - pe) / w).max() < 1e-2, (k, (pts[k] - pe) / w)
+    if fu_case[5].get("unimodal"):
+        assert not parted, parted
+    print("\nascent %s %s: vs FP64-oracle ascent max rel F diff %.2e, max point diff %.2e widths, "
+          "max |w grad|/F at the end %.2e, paths ending on another maximum %s"
+          % (form, fu_case[5]["name"], worst_f, worst_p, worst_g, parted))
