@@ -93,6 +93,49 @@ int pa_coinc_main(int argc, char **argv);
 int pa_fisher_reduced(const double *rSSB, const double *rDet, long long n, double epsm, double xi,
                       double *fisher);
 
+/* Input generation: the grid generator's lattice (gridgen/main.cpp:955-1166
+ * with GridS2.cpp, DensityS1.cpp, GridS1.cpp and num.cpp), i.e. the
+ * grid.bin of a data segment, from the same ephemeris contents as
+ * pa_fisher_reduced (rSSB, rDet: n x 3 doubles; epsm from DetSSB.bin).
+ * Equal to the grid generator's grid.bin bit for bit. */
+typedef struct pa_gridgen_opts {
+  double c0;           /* covering parameter, minimal match squared (-c; the
+                          generator's -m m sets c0 = m*m printed with six
+                          decimals, main.cpp:172-190) */
+  double xi;           /* initial time (-i, default 0.5) */
+  int nfft_exp;        /* log2 of the FFT length (-n) */
+  int method;          /* 0 automatic (main.cpp:1578-1606), 1 the A4* lattice
+                          S1, 2 the tilted cell S2 (-a) */
+  int nalpha, nradius; /* bisection and deep-hole depths of S2 (-na, -nr;
+                          defaults 35, 20) */
+  const char *table;   /* the generator's table of S2 cells, dataS2.txt
+                          (read from its working directory); NULL: none */
+} pa_gridgen_opts;
+
+typedef struct pa_gridgen_out {
+  int fftpad;          /* log2(nfft) - ceil(log2(n)) + 1 */
+  double M[16];        /* grid-generating matrix as grid.bin stores it */
+  double fisher[16];   /* reduced Fisher matrix at xi */
+  double Mn[16];       /* the matrix before the division by n */
+  int method;          /* 1 or 2, as chosen */
+  double alpha;        /* S2: the cell's tilt */
+  int alpha_from_table;/* S2: the tilt came from the table */
+  double density;      /* density of covering of the basis (printed by the
+                          generator) */
+} pa_gridgen_out;
+
+/* Returns PA_OK, or PA_ERR_ARG for n < 5, n > nfft, c0 outside (0, 1) or an
+ * unknown method.  S1: among lattice vectors of exactly equal length the
+ * first in enumeration order is taken (the generator's std::sort leaves that
+ * order unspecified).  The table is read, never written (the generator
+ * appends newly computed cells to its copy). */
+int pa_gridgen(const double *rSSB, const double *rDet, long long n, double epsm, const pa_gridgen_opts *opts,
+               pa_gridgen_out *out);
+
+/* Writes the 388-byte grid.bin: int fftpad, then M, fisher and Mn (16
+ * doubles each, main.cpp:1042-1160). */
+int pa_gridgen_write(const char *path, const pa_gridgen_out *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,5 +1,5 @@
-"""Build recipe of libpolgraw_gb300.so and the gwsearch-gb300 and
-coincidences-gb300 programs.
+"""Build recipe of libpolgraw_gb300.so and the gwsearch-gb300,
+coincidences-gb300 and gridgen-gb300 programs.
 
 nvcc compiles the CUDA translation units for sm_103a only
 (-gencode arch=compute_103a,code=sm_103a); gcc compiles the C host.  Host
@@ -20,11 +20,12 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libpolgraw_gb300.so")
 EXE = os.path.join(BUILD, "gwsearch-gb300")
 COINC_EXE = os.path.join(BUILD, "coincidences-gb300")
+GRIDGEN_EXE = os.path.join(BUILD, "gridgen-gb300")
 INCLUDE = os.path.join(ROOT, "include")
 
 CU_SOURCES = ["csrc/pa_engine_f32.cu", "csrc/pa_engine_f32_f64phase.cu", "csrc/pa_engine_f32_ffphase.cu",
               "csrc/pa_engine_f64.cu", "csrc/pa_api.cu", "csrc/pa_followup.cu", "csrc/pa_coinc.cu"]
-C_SOURCES = ["host/pa_host.c", "host/pa_coinc_host.c", "host/pa_grid.c"]
+C_SOURCES = ["host/pa_host.c", "host/pa_coinc_host.c", "host/pa_grid.c", "host/pa_lattice.c"]
 HEADERS = ["csrc/pa_fft.cuh", "csrc/pa_engine.cuh", "csrc/pa_engine.h", "csrc/pa_trace.h"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE]
@@ -94,7 +95,8 @@ def build(force: bool = False, verbose: bool = False, trace: bool = False) -> st
         os.replace(tmp, lib_path)
     if trace:
         return lib_path
-    for exe, main in ((EXE, "gwsearch_gb300.c"), (COINC_EXE, "coincidences_gb300.c")):
+    for exe, main in ((EXE, "gwsearch_gb300.c"), (COINC_EXE, "coincidences_gb300.c"),
+                      (GRIDGEN_EXE, "gridgen_gb300.c")):
         main_src = os.path.join(HERE, "host", main)
         if force or _stale(exe, [LIB, main_src]):
             _run(["gcc"] + CC_FLAGS + ["-o", exe, main_src, "-L" + BUILD, "-lpolgraw_gb300",

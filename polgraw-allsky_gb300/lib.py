@@ -39,7 +39,7 @@ EXPORTS = [
     "pa_coinc_vedva", "pa_coinc_create", "pa_coinc_destroy", "pa_coinc_last_error", "pa_coinc_reset",
     "pa_coinc_add_frame", "pa_coinc_run", "pa_coinc_get", "pa_coinc_cells", "pa_coinc_last_call_ms",
     "pa_coinc_kernel_launches", "pa_coinc_main", "pa_coinc_set_profiling", "pa_coinc_profile_get",
-    "pa_fisher_reduced",
+    "pa_fisher_reduced", "pa_gridgen", "pa_gridgen_write",
 ]
 
 
@@ -188,6 +188,9 @@ def load(path: str | None = None) -> C.CDLL:
     lib.pa_coinc_kernel_launches.argtypes = [C.c_void_p]
     lib.pa_fisher_reduced.argtypes = [P(C.c_double), P(C.c_double), C.c_longlong, C.c_double, C.c_double,
                                       P(C.c_double)]
+    lib.pa_gridgen.argtypes = [P(C.c_double), P(C.c_double), C.c_longlong, C.c_double, P(GridgenOpts),
+                               P(GridgenOut)]
+    lib.pa_gridgen_write.argtypes = [C.c_char_p, P(GridgenOut)]
     lib.pa_coinc_set_profiling.argtypes = [C.c_void_p, C.c_int]
     lib.pa_coinc_profile_get.argtypes = [C.c_void_p, C.c_int, P(C.c_char_p), P(C.c_double), P(C.c_longlong)]
     lib.pa_host_create.restype = C.c_void_p
@@ -688,6 +691,36 @@ def fisher_reduced(rssb, rdet, epsm: float, xi: float = 0.5) -> np.ndarray:
     if rc != PA_OK:
         raise SearchError("pa_fisher_reduced failed (%d)" % rc)
     return out.reshape(4, 4)
+
+
+class GridgenOpts(C.Structure):
+    _fields_ = [("c0", C.c_double), ("xi", C.c_double), ("nfft_exp", C.c_int), ("method", C.c_int),
+                ("nalpha", C.c_int), ("nradius", C.c_int), ("table", C.c_char_p)]
+
+
+class GridgenOut(C.Structure):
+    _fields_ = [("fftpad", C.c_int), ("M", C.c_double * 16), ("fisher", C.c_double * 16), ("Mn", C.c_double * 16),
+                ("method", C.c_int), ("alpha", C.c_double), ("alpha_from_table", C.c_int), ("density", C.c_double)]
+
+    def grid_bin(self) -> bytes:
+        """The 388 bytes of grid.bin."""
+        import struct
+        return struct.pack("<i", self.fftpad) + b"".join(
+            np.array(list(m), dtype="<f8").tobytes() for m in (self.M, self.fisher, self.Mn))
+
+
+def gridgen(rssb, rdet, epsm: float, nfft_exp: int, c0: float = 0.5625, xi: float = 0.5, method: int = 0,
+            nalpha: int = 35, nradius: int = 20, table: str | None = None) -> GridgenOut:
+    """pa_gridgen: the grid generator's grid.bin contents from the ephemeris
+    parts (n x 3 each)."""
+    a = np.ascontiguousarray(np.asarray(rssb, dtype=np.float64).reshape(-1))
+    b = np.ascontiguousarray(np.asarray(rdet, dtype=np.float64).reshape(-1))
+    o = GridgenOpts(c0, xi, nfft_exp, method, nalpha, nradius, table.encode() if table else None)
+    out = GridgenOut()
+    rc = load().pa_gridgen(_dp(a), _dp(b), len(a) // 3, epsm, C.byref(o), C.byref(out))
+    if rc != PA_OK:
+        raise SearchError("pa_gridgen failed (%d)" % rc)
+    return out
 
 
 def vedva(fisher) -> np.ndarray:
