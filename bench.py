@@ -56,9 +56,9 @@ NSKY_DEFAULT = 2000
 NSPIN_DEFAULT = 200
 
 
-def make_workload(root: str, nspin: int):
+def make_workload(root: str, nspin: int, npoints: int = NSKY_DEFAULT):
     """Writes the data set and returns the search command line."""
-    return workloads.network(root, nspin)[0]
+    return workloads.network(root, nspin, npoints)[0]
 
 
 def sky_tasks(host, limit: int):
@@ -785,24 +785,26 @@ def main():
             run_coinc(args, L)
         return
     tmp = tempfile.mkdtemp(prefix="pa_bench_")
-    argv = make_workload(tmp, args.spindowns)
+    # N > 1: the sky partitioned over the GPUs (weak scaling: a lattice of
+    # about args.sky x N points, each rank a contiguous block of args.sky of
+    # them; sky points are independent, nothing is exchanged); the step time
+    # is the maximum over ranks and the work the sum
+    from polgraw_gb300 import shards
+    argv = make_workload(tmp, args.spindowns, args.sky if world == 1 else int(args.sky * world * 1.03) + 1)
     host = L.Host(argv)
-    tasks = sky_tasks(host, args.sky)
+    tasks = shards.shard(sky_tasks(host, args.sky * world), rank, world, args.sky)
     s = host.settings
     bins = s.nmax - s.nmin
     nspin = args.spindowns
     cfg = {"workload": WORKLOAD, "sky_points": len(tasks), "spindowns": nspin, "bins": bins,
            "graphs": bool(args.graphs),
            "nifo": 2, "N": s.N, "nfftf": s.nfftf, "phase": args.phase,
-           "l2": "flushed (256 MB write) before each timed step", "parallelism": "replicas" if world > 1 else "1 GPU"}
+           "l2": "flushed (256 MB write) before each timed step",
+           "parallelism": ("sky partitioned over %d GPUs, %d sky points each, no collective in the search"
+                           % (world, args.sky)) if world > 1 else "1 GPU"}
 
-
-    # N > 1: one replica of the whole workload per GPU (sky points are
-    # independent, nothing is exchanged); the step time is the maximum over
-    # ranks and the work the sum (weak scaling)
-    from polgraw_gb300 import replicas
-    replicas.init()
-    local = replicas.world()[2]
+    shards.init()
+    local = shards.world()[2]
     device = local if world > 1 else 0
     if world > 1:
         import torch
@@ -828,10 +830,10 @@ def main():
         if rank == 0:
             emit(run_cta_trace(ctx, tasks, opts, rng, cfg, nspin * bins))
         ctx.close()
-        replicas.shutdown()
+        shards.shutdown()
         return
     launches0 = ctx.launches()
-    replicas.barrier()
+    shards.barrier()
     clocks = ClockSampler(device)
     dev_ms = []
     ncand = 0
@@ -840,22 +842,22 @@ def main():
         rec, idx, fnum = ctx.search_batch(tasks, opts, rng)
         dev_ms.append(ctx.last_call_ms())
         ncand = len(rec)
-    replicas.barrier()
+    shards.barrier()
     clk = clocks.stop()
     launches = (ctx.launches() - launches0) // max(1, args.steps)
-    t_dev, templates_all = replicas.reduce_step(sum(dev_ms) / 1e3, float(templates))
+    t_dev, templates_all = shards.reduce_step(sum(dev_ms) / 1e3, float(templates))
     value = templates_all * args.steps / t_dev
 
     # end to end: host buffers in, candidates out, through the C-ABI
     e2e_t = 0.0
-    replicas.barrier()
+    shards.barrier()
     for _ in range(args.steps):
         l2_flush()
         t0 = time.perf_counter()
         ctx.set_data(dets, nifo)
         rec, idx, fnum = ctx.search_batch(tasks, opts, rng)
         e2e_t += time.perf_counter() - t0
-    e2e_t, _ = replicas.reduce_step(e2e_t, 0.0)
+    e2e_t, _ = shards.reduce_step(e2e_t, 0.0)
     e2e = templates_all * args.steps / e2e_t
     h2d = nifo * s.N * 8 * 4
     d2h = 4 + len(rec) * 24
@@ -951,7 +953,7 @@ def main():
     if rank == 0:
         emit(out)
     ctx.close()
-    replicas.shutdown()
+    shards.shutdown()
 
 
 if __name__ == "__main__":

@@ -10,7 +10,8 @@ import name ``polgraw_gb300`` by a path loader (see ``load_package`` in
 * ``synth`` -- synthetic inputs in the reference's on-disk layout
 * ``workloads`` -- the benchmark's synthetic workloads (network, precision
                stress, segments, followup, coincidences)
-* ``replicas`` -- reduction of per-GPU replica timings under torchrun
+* ``shards`` -- the sky partitioned over GPUs under torchrun, and the
+               reduction of the ranks' timings
 
 The reference host set-up itself (settings, data reading, injection,
 ranges) is C, in host/pa_host.c; ``lib.Host`` binds it.

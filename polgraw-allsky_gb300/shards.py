@@ -1,10 +1,13 @@
-"""Multi-GPU runs of the search: replicas.
+"""Multi-GPU runs of the search: the sky partitioned over the GPUs.
 
 Sky points are independent and the search has no exchange step, so N GPUs
-run N replicas (one process per GPU, each with its own context and its own
-copy of the workload) and the only communication is the timing reduction of
-the benchmark: the step time is the maximum over ranks and the work the sum
-over ranks.  torch.distributed carries it (NCCL between GPUs, gloo on CPU).
+split the sky as the reference splits it over processes with -range files
+(search/network/src-cpu/init.c:664-700): each rank (one process per GPU,
+its own context and copy of the detector data) takes a contiguous block of
+sky points in the sky loop's order (contiguous mm ranges), and the only
+communication is the benchmark's timing reduction: the step time is the
+maximum over ranks and the work the sum over ranks.  torch.distributed
+carries it (NCCL between GPUs, gloo on CPU).
 """
 from __future__ import annotations
 
@@ -30,6 +33,21 @@ def init(backend: str | None = None) -> bool:
     os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
     dist.init_process_group(backend=backend, rank=rank, world_size=size)
     return True
+
+
+def shard(tasks: list, rank: int, size: int, per_rank: int | None = None) -> list:
+    """The rank's contiguous block of the sky points `tasks` (in sky-loop
+    order): blocks of `per_rank` points (default: len(tasks) // size, the
+    last rank taking the remainder); blocks of different ranks are
+    disjoint."""
+    if size <= 1:
+        return list(tasks if per_rank is None else tasks[:per_rank])
+    if per_rank is None:
+        per = len(tasks) // size
+        lo = rank * per
+        hi = len(tasks) if rank == size - 1 else lo + per
+        return list(tasks[lo:hi])
+    return list(tasks[rank * per_rank:(rank + 1) * per_rank])
 
 
 def barrier() -> None:

@@ -49,9 +49,10 @@ def _lattice(root, *, dt, nod, band, fftpad, m5, npoints, dets=("H1", "L1")):
     return ds, nmax
 
 
-def network(root: str, nspin: int = 200):
-    """The H1+L1 N=86164 network workload (2000 sky x `nspin` spindowns)."""
-    ds, nmax = _lattice(root, dt=2.0, nod=2, band=666, fftpad=1, m5=-1e-9, npoints=2000)
+def network(root: str, nspin: int = 200, npoints: int = 2000):
+    """The H1+L1 N=86164 network workload (a lattice of about `npoints` sky
+    points on one hemisphere, 2000 by default, x `nspin` spindowns)."""
+    ds, nmax = _lattice(root, dt=2.0, nod=2, band=666, fftpad=1, m5=-1e-9, npoints=npoints)
     inj = _inject_random(ds, np.random.default_rng(2002), 5, fdot_lo=-1.9e-7, fdot_hi=0.0,
                          snr_lo=8, snr_hi=15)
     rpath = os.path.join(root, "range.txt")
