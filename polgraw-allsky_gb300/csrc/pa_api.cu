@@ -1023,7 +1023,7 @@ int pa_autotune(pa_ctx* c, const pa_sky* tasks, int ntasks, const pa_opts* o, co
       c->b.sbatch = sb;
       c->eng->set_split(sp);
       double t = 1e300;
-      for (int rep = 0; rep < 3; rep++) {  // first run warms up
+      for (int rep = 0; rep < 4; rep++) {  // first run warms up; best of three
         int rc = run_tasks(c, hs, o, &out);
         if (rc) {
           c->lanes = ln0;

@@ -136,6 +136,8 @@ CASES = [
 # from offset starting points.
 #   fu_h1l1v1   three detectors (H1, L1, V1), N=10771 (1 day at dt=8 s)
 #   fu_h1l1_dt2 two detectors (H1, L1), N=43082 (1 day at dt=2 s), southern sky
+#   fu_h1l1v1_n86164 the followup configuration's size: three detectors
+#               (H1, L1, V1), N=86164 (2 sidereal days at dt=2 s)
 FOLLOWUP_CASES = [
     dict(name="fu_h1l1v1",
          data=dict(dets=["H1", "L1", "V1"], dt=8.0, nod=1, band=100, fftpad=1,
@@ -151,6 +153,15 @@ FOLLOWUP_CASES = [
          range=[0, 0, 0, 0, 0, 0, None, None],
          # local maxima of F (about 151.6 and 102) lie within 0.5 peak widths
          # of the peak (152.1): an ascent from a nearby start may stop there
+         unimodal=False),
+    dict(name="fu_h1l1v1_n86164",
+         data=dict(dets=["H1", "L1", "V1"], dt=2.0, nod=2, band=666, fftpad=1,
+                   grid=dict(m5=-1e-9, sky_scale=0.05)),
+         inject=dict(f=1.5, fdot=-5e-9, delta=0.2, alpha=3.0, snr=20.0),
+         range=[0, 0, 0, 0, 0, 0, None, None],
+         # a long ridge through the peak (172.4: ascents from nearby starts
+         # stall on it near 172.2) and a far side maximum near 46 reached
+         # from a start at F = 3
          unimodal=False),
 ]
 

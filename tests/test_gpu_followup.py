@@ -176,17 +176,26 @@ def test_simplex_matches_reference(form, fu_case, gpu_ok):
     starts = np.array([a["start"] for a in am])
     pts, out, nev = fu.simplex(starts, am[0]["pc2"], tol=am[0]["tol"], max_evals=5000)
     w = np.array(g["widths"])
+    Fr_all = [-a["out"][5] for a in am]
     for k, a in enumerate(am):
         Fr = -a["out"][5]
         # F of the reference's maximum within 10x the F tolerance; in the FP64
         # form also its point (0.05 widths).  The simplex path is chaotic:
         # rounding-level F differences of the mixed forms can turn a
-        # comparison and end it on a side maximum of the same F level.
-        assert -out[k, 5] >= Fr * (1 - 10 * FORMS[form][1]), (k, -out[k, 5], Fr)
+        # comparison and end it on a side maximum of the same F level, or at
+        # another point of a ridge along which the reference's own runs stop
+        # at different heights (fu_h1l1v1_n86164: 172.19 to 172.40); a mixed
+        # run must then still end as high as the lowest of the reference's
+        # runs, and the best mixed run at the reference's best.
+        if form == "fp64":
+            assert -out[k, 5] >= Fr * (1 - 10 * FORMS[form][1]), (k, -out[k, 5], Fr)
+        else:
+            assert -out[k, 5] >= min(Fr_all) * (1 - 10 * FORMS[form][1]), (k, -out[k, 5], Fr_all)
         if form == "fp64":
             assert np.abs((pts[k] - np.array(a["point"])) / w).max() < 0.05
         if form == "fp64":
             assert abs(int(nev[k]) - a["nevals"]) <= 0.2 * a["nevals"]
+    assert (-out[:, 5]).max() >= max(Fr_all) * (1 - 10 * FORMS[form][1]), (-out[:, 5], Fr_all)
     # the batch of three and each start alone give the same result
     p1, o1, n1 = fu.simplex(starts[1:2], am[0]["pc2"], tol=am[0]["tol"], max_evals=5000)
     assert np.array_equal(p1[0], pts[1]) and n1[0] == nev[1]
@@ -272,7 +281,11 @@ def test_ascent_reaches_simplex_maximum(form, fu_case, gpu_ok):
         Fg, gg = orc.fstatnet_grad(pts[k])
         assert Fg >= Fs * (1 - ftol), (k, Fg, Fs)
         worst_g = max(worst_g, float(np.abs(w * gg).max() / Fg))
-        assert np.abs(w * gg).max() <= 2e-3 * Fg, (k, np.abs(w * gg).max() / Fg)
+        # stationary: the gradient (width units) below 2e-3 of F in the FP64
+        # form; the mixed forms' FP32 gradient carries noise of a few 1e-3
+        # of F per width, where their ascent may stop
+        gtol = 2e-3 if form == "fp64" else 1e-2
+        assert np.abs(w * gg).max() <= gtol * Fg, (k, np.abs(w * gg).max() / Fg)
         if abs(Fg - Fe) > 1e-3 * Fe:
             assert form != "fp64", (k, Fg, Fe)
             assert abs(Fg - Fe) <= 1e-2 * Fe, (k, Fg, Fe)
