@@ -306,6 +306,35 @@ struct SpinCta {
   float s1h, s1l, h1h, h1l;
 };
 
+// Most spindowns in one launch of the spindown passes (the buffers are sized
+// for at most 128).
+constexpr int kSpinBatchMax = 128;
+
+// het1 = fmod(ss M4, M0), wrapped into [0, M0) (jobcore.c:466-467), as
+// 64-bit fixed-point turns: round-to-nearest-even of het1 2^64 / (2 pi),
+// saturated as __double2ull_rn does.  fmod is exact and the two products
+// are single roundings, so the host and the device give the same bits.
+inline uint64_t het1_turns_fixed(int ss, double M4, double M0) {
+  double het1 = fmod(ss * M4, M0);
+  if (het1 < 0) het1 += M0;
+  const double x = het1 * kTurnsPerRad64;
+  if (!(x > 0.)) return 0;
+  if (x >= 18446744073709551616.0) return ~0ull;
+  return (uint64_t)nearbyint(x);
+}
+
+// Per-launch spindown constants passed by value with the loader.  The
+// fixed-point form takes the het1 term of each batch item from the host
+// (H[batch]), so that no CTA of pass A waits on a chain of FP64 operations
+// before its first phase; the other forms form theirs per CTA (prologue).
+template <typename R, int PM> struct SpinHet {
+  static constexpr bool kHost = false;
+};
+template <> struct SpinHet<float, PM_FIXED> {
+  static constexpr bool kHost = true;
+  unsigned long long H[kSpinBatchMax];
+};
+
 // (a * b) mod 2^64 for a 64-bit a and a 32-bit b
 __device__ __forceinline__ uint64_t mul64x32(uint64_t a, unsigned b) {
   return (uint64_t)(unsigned)a * b + ((uint64_t)((unsigned)(a >> 32) * b) << 32);
@@ -316,13 +345,31 @@ __device__ __forceinline__ uint64_t mul64x32(uint64_t a, unsigned b) {
 template <typename R, int PM> struct SpinLoader {
   typedef typename CT<R>::T T;
   static constexpr int kTraceKind = KK_SPIN_A;
+  // the fixed-point form needs no shared-memory constants (no barrier after
+  // the prologue)
+  static constexpr bool kPrologue = !SpinHet<R, PM>::kHost;
   const T* xm;       // [nifo][2][N]
   const void* ph0;   // FP64 form: tmp1 [nifo][N]; FP32 forms: unused
   int N, nifo, ss0, ss_base, s0_flag;
   double M0, M4, M5, s1_0;
+  SpinHet<R, PM> het;
+
+  // Spindown constants of batch item `batch`: the fixed-point form's from
+  // the launch parameters (registers), the other forms' from the prologue's
+  // shared-memory copy.
+  __device__ __forceinline__ SpinCta consts(int batch, const char* sm) const {
+    SpinCta k;
+    if constexpr (SpinHet<R, PM>::kHost) {
+      k.H = het.H[batch];
+      k.ssr = s0_flag ? 0u : (unsigned)(ss0 + batch - ss_base);
+    } else {
+      k = *reinterpret_cast<const SpinCta*>(sm);
+    }
+    return k;
+  }
 
   __device__ __forceinline__ void prologue(int batch, char* sm) const {
-    if (threadIdx.x == 0) {
+    if (kPrologue && threadIdx.x == 0) {
       SpinCta* p = reinterpret_cast<SpinCta*>(sm);
       const int ss = ss0 + batch;
       double het1 = fmod(ss * M4, M0);
@@ -339,10 +386,11 @@ template <typename R, int PM> struct SpinLoader {
     }
   }
 
-  __device__ __forceinline__ void load2(int, int n, T& va, T& vb, const char* sm) const {
+  __device__ __forceinline__ void load2(int batch, int n, T& va, T& vb, const char* sm) const {
     va = vb = mk((R)0, (R)0);
     if (n >= N) return;
-    const SpinCta* p = reinterpret_cast<const SpinCta*>(sm);
+    const SpinCta pk = consts(batch, sm);
+    const SpinCta* p = &pk;
     R accx = 0, accy = 0, bccx = 0, bccy = 0;
     double base = 0.;
     uint64_t ibase = 0;
@@ -430,9 +478,9 @@ template <typename R, int PM> struct SpinLoader {
 
   // One detector's term of load2 (FP32 forms, n < N): xm_{a,b,d}[n] times
   // exp(-i phase_d(n)), with the phase evaluated as load2 does.
-  __device__ __forceinline__ void mod1(int d, int n, T& pa, T& pb, const char* sm) const {
+  __device__ __forceinline__ void mod1(int d, int n, T& pa, T& pb, const SpinCta& pk) const {
     static_assert(sizeof(R) == 4, "FP32 forms only");
-    const SpinCta* p = reinterpret_cast<const SpinCta*>(sm);
+    const SpinCta* p = &pk;
     const size_t o = (size_t)d * N + n;
     const float4 lo16 = __ldg(reinterpret_cast<const float4*>(xm) + 2 * o);
     const uint4 hi16 = __ldg(reinterpret_cast<const uint4*>(xm) + 2 * o + 1);
@@ -492,7 +540,8 @@ template <typename R, int PM> struct SpinLoader {
 // 2 per c makes the stage-2 reads conflict-free (half-warp slots 2c + arr).
 template <int SIGN, int LOGL, int PM>
 __global__ void __launch_bounds__(512, 2)
-    k_pass_a16(const SpinLoader<float, PM> ld, const float2* __restrict__ tw1, const float2* __restrict__ twlo,
+    k_pass_a16(const __grid_constant__ SpinLoader<float, PM> ld, const float2* __restrict__ tw1,
+               const float2* __restrict__ twlo,
                const float2* __restrict__ twhi, float2* __restrict__ ybuf) {
   constexpr int LOGL1 = 8, LOGL2 = LOGL - LOGL1, ZC = 16 * 32 + 2;
   constexpr int Lmask = (1 << LOGL) - 1;
@@ -507,6 +556,7 @@ __global__ void __launch_bounds__(512, 2)
   for (int m = threadIdx.x; m < 256; m += 512) tws[m] = tw1[m];
   ld.prologue(batch, lsm);
   __syncthreads();
+  const SpinCta pk = ld.consts(batch, lsm);
   float2 v[16];
   {
     const int arr = lane & 1;
@@ -515,7 +565,7 @@ __global__ void __launch_bounds__(512, 2)
     for (int a = 0; a < 16; ++a) {
       const int n = ((16 * a + w) << LOGL2) + n2;
       float2 pa = make_float2(0.f, 0.f), pb = pa;
-      if (n < ld.N) ld.mod1(arr, n, pa, pb, lsm);
+      if (n < ld.N) ld.mod1(arr, n, pa, pb, pk);
       const float2 send = arr ? pa : pb;
       const float2 mine = arr ? pb : pa;
       const float rx = __shfl_xor_sync(0xffffffffu, send.x, 1);
@@ -1269,6 +1319,10 @@ template <typename R, int PM> class EngineT : public Engine {
     sl.M4 = sky.M4;
     sl.M5 = sky.M5;
     sl.s1_0 = sky.s1_0;
+    if (nb > kSpinBatchMax) return cudaErrorInvalidValue;
+    if constexpr (SpinHet<R, PM>::kHost) {
+      for (int k = 0; k < nb; ++k) sl.het.H[k] = het1_turns_fixed(ss0 + k, sky.M4, sky.M0);
+    }
     FstatStore<R> fs{Fl, (const R*)b_.sums_r[slot], b_.nmin, b_.nmax, b_.bins};
     cudaError_t e = fft<-1, true>(gm_, b_.tw_main, sl, fs, nb, st, KK_SPIN_A, KK_SPIN_B, yb, split_);
     if (e != cudaSuccess) return e;

@@ -394,7 +394,7 @@ struct CtaTrace {
 // Loader: prologue(batch, smem scratch) and load2(batch, n, a, b, scratch).
 template <typename R, int SIGN, int LOGL, class Loader, int SPLIT = 0>
 __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
-    k_pass_a(const Loader ld, const typename CT<R>::T* __restrict__ tw1,
+    k_pass_a(const __grid_constant__ Loader ld, const typename CT<R>::T* __restrict__ tw1,
              const typename CT<R>::T* __restrict__ twlo, const typename CT<R>::T* __restrict__ twhi,
              typename CT<R>::T* __restrict__ ybuf) {
   typedef typename CT<R>::T T;
