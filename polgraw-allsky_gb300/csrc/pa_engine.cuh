@@ -260,6 +260,7 @@ __global__ void __launch_bounds__(256)
 template <typename R> struct PlainLoader {
   typedef typename CT<R>::T T;
   static constexpr int kTraceKind = KK_FFT_FWD_A;
+  static constexpr bool kEarlyLoads = true;  // no prologue: loads before any barrier
   const T* in;   // [batch][2][ld]
   int len, ld;
   __device__ __forceinline__ void prologue(int, char*) const {}
@@ -286,6 +287,7 @@ template <typename R> struct PlainLoader {
 template <typename R> struct HalfShiftLoader {
   typedef typename CT<R>::T T;
   static constexpr int kTraceKind = KK_FFT_INV_A;
+  static constexpr bool kEarlyLoads = true;  // no prologue: loads before any barrier
   const T* spec;    // [batch][2][nfft]
   const T* twlo;    // e^{+2 pi i m/Ninterp}, m < 1024
   const T* twhi;    // e^{+2 pi i 1024 m/Ninterp}
@@ -348,6 +350,8 @@ template <typename R, int PM> struct SpinLoader {
   // the fixed-point form needs no shared-memory constants (no barrier after
   // the prologue)
   static constexpr bool kPrologue = !SpinHet<R, PM>::kHost;
+  // generic pass A: first loads before any barrier (no prologue to wait for)
+  static constexpr bool kEarlyLoads = !kPrologue;
   const T* xm;       // [nifo][2][N]
   const void* ph0;   // FP64 form: tmp1 [nifo][N]; FP32 forms: unused
   int N, nifo, ss0, ss_base, s0_flag;

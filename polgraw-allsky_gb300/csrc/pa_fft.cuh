@@ -249,8 +249,14 @@ __device__ __forceinline__ void stage_mid(T* s, const T* tw) {
 
 // First stage (Ns = 1, no twiddles) from values produced by `src(e, c, a, b)`
 // in registers, written to shared memory (c-fastest mapping).
-template <int SIGN, int RAD, int E, int NT, int LOGL, int LOGCS, int P, class T, class Src>
-__device__ __forceinline__ void stage_first(T* s, const Src& src) {
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
+// (hook: shared-memory stores of the caller that the later stages read,
+// issued just before this stage's barrier)
+template <int SIGN, int RAD, int E, int NT, int LOGL, int LOGCS, int P, class T, class Src, class Hook = NoHook>
+__device__ __forceinline__ void stage_first(T* s, const Src& src, const Hook& hook = Hook()) {
   constexpr int PPT = E / (2 * RAD * NT);
   constexpr int logLR = LOGL - LogR<RAD>::v;
 #pragma unroll
@@ -265,6 +271,7 @@ __device__ __forceinline__ void stage_first(T* s, const Src& src) {
 #pragma unroll
     for (int r = 0; r < RAD; ++r) Pair<T>::st(s + (j * RAD + r) * P + 2 * c, va[r], vb[r]);
   }
+  hook();
   __syncthreads();
 }
 
@@ -285,9 +292,9 @@ template <int LOGL> struct FirstRadix {
 };
 
 // First stage and middle stages; the last radix-8 stage has Ns = L/8.
-template <int SIGN, int E, int NT, int LOGL, int LOGCS, int P, class T, class Src>
-__device__ __forceinline__ void fft_front(T* s, const T* tw, const Src& src) {
-  stage_first<SIGN, FirstRadix<LOGL>::v, E, NT, LOGL, LOGCS, P>(s, src);
+template <int SIGN, int E, int NT, int LOGL, int LOGCS, int P, class T, class Src, class Hook = NoHook>
+__device__ __forceinline__ void fft_front(T* s, const T* tw, const Src& src, const Hook& hook = Hook()) {
+  stage_first<SIGN, FirstRadix<LOGL>::v, E, NT, LOGL, LOGCS, P>(s, src, hook);
   stages_mid<SIGN, E, NT, LOGL, LOGCS, P, FirstRadix<LOGL>::logv>(s, tw);
 }
 
@@ -407,11 +414,22 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
   char* lsm = reinterpret_cast<char*>(tws + G::L1);   // loader scratch
   const int batch = blockIdx.y;
   const int c0 = blockIdx.x << G::LOGC;
-  for (int m = threadIdx.x; m < G::L1; m += NT) tws[m] = tw1[m];
-  ld.prologue(batch, lsm);
-  __syncthreads();
   auto src = [&](int n1, int c, T& a, T& b) { ld.load2(batch, (n1 << G::LOGL2) + c0 + c, a, b, lsm); };
-  fft_front<SIGN, E, NT, G::LOGL1, G::LOGC, P>(s, tws, src);
+  if constexpr (Loader::kEarlyLoads && G::L1 <= NT) {
+    // no loader constants in shared memory: the column twiddles are stored
+    // at the end of the first stage (as in pass B), no barrier before the
+    // first loads
+    const T twv = threadIdx.x < G::L1 ? tw1[threadIdx.x] : T();
+    auto fill = [&]() {
+      if (threadIdx.x < G::L1) tws[threadIdx.x] = twv;
+    };
+    fft_front<SIGN, E, NT, G::LOGL1, G::LOGC, P>(s, tws, src, fill);
+  } else {
+    for (int m = threadIdx.x; m < G::L1; m += NT) tws[m] = tw1[m];
+    ld.prologue(batch, lsm);
+    __syncthreads();
+    fft_front<SIGN, E, NT, G::LOGL1, G::LOGC, P>(s, tws, src);
+  }
   // last radix-8 stage, lanes along j (= k1 mod Ns)
   constexpr int LOGNS = G::LOGL1 - 3, Ns = 1 << LOGNS;
   constexpr int PPT = E / (2 * 8 * NT);
@@ -454,14 +472,25 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
   // last, so their intermediate is the likeliest to be still in L2
   const int batch = gridDim.y - 1 - blockIdx.y;
   const int k10 = blockIdx.x << G::LOGRR;
-  for (int m = threadIdx.x; m < G::L2; m += NT) tws[m] = tw2[m];
   const T* yb = ybuf + ((size_t)batch << (LOGL + 1));
   // the intermediate is read once, here: evict-first
   auto src = [&](int n2, int rr, T& a, T& b) {
     Pair<T>::ldlast(yb + (((size_t)n2 << G::LOGL1) + k10 + rr) * 2, a, b);
   };
-  __syncthreads();
-  fft_front<SIGN, E, NT, G::LOGL2, G::LOGRR, P>(s, tws, src);
+  if constexpr (G::L2 <= NT) {
+    // one twiddle per thread, loaded first and stored to shared memory at
+    // the end of the first stage (which does not use it), so that the
+    // intermediate's loads are not held behind a barrier
+    const T twv = threadIdx.x < G::L2 ? tw2[threadIdx.x] : T();
+    auto fill = [&]() {
+      if (threadIdx.x < G::L2) tws[threadIdx.x] = twv;
+    };
+    fft_front<SIGN, E, NT, G::LOGL2, G::LOGRR, P>(s, tws, src, fill);
+  } else {
+    for (int m = threadIdx.x; m < G::L2; m += NT) tws[m] = tw2[m];
+    __syncthreads();
+    fft_front<SIGN, E, NT, G::LOGL2, G::LOGRR, P>(s, tws, src);
+  }
   constexpr int LOGNS = G::LOGL2 - 3, Ns = 1 << LOGNS;
   constexpr int PPT = E / (2 * 8 * NT);
 #pragma unroll
