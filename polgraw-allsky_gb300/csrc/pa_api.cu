@@ -77,7 +77,9 @@ struct pa_ctx {
 static int active_lanes(const pa_ctx* c) { return c->prof.on ? 1 : c->lanes; }
 static cudaStream_t prelude_stream(const pa_ctx* c) { return c->prof.on ? c->stream : c->stream_pre; }
 
-// sky points per captured part of a batch (launch_tasks)
+// sky points per captured part of a batch (launch_tasks): the first part
+// kGraphFirst, each next one twice the previous, up to kGraphPart
+constexpr size_t kGraphFirst = 16;
 constexpr size_t kGraphPart = 256;
 
 static void drop_graphs(pa_ctx* c) {
@@ -769,17 +771,22 @@ int launch_tasks(pa_ctx* c, const std::vector<SkyHost>& hs, const pa_opts* o) {
     CK(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
     return enqueue_tasks(c, hs, o);
   }
-  // The batch is captured in parts of about kGraphPart sky points, each into
-  // its own executable graph (updated in place when the part's launch
-  // structure repeats), and each part is launched as soon as it is captured:
-  // the host captures part k + 1 while the device runs part k, so only the
-  // first part's capture precedes device work.
+  // The batch is captured in parts, each into its own executable graph
+  // (updated in place when the part's launch structure repeats), and each
+  // part is launched as soon as it is captured: the host captures part k + 1
+  // while the device runs part k.  Only the first part's capture precedes
+  // device work, so it is short (kGraphFirst sky points); the parts then
+  // double, as capturing a sky point takes the host far less time than the
+  // device takes to search it, up to kGraphPart.
   const size_t n = hs.size();
-  const size_t nparts = std::max<size_t>(1, (n + kGraphPart - 1) / kGraphPart);
-  const size_t per = (n + nparts - 1) / nparts;
+  std::vector<size_t> bound{0};
+  for (size_t step = kGraphFirst; bound.back() < n; step = std::min(kGraphPart, 2 * step))
+    bound.push_back(std::min(n, bound.back() + step));
+  if (n == 0) bound.push_back(0);
+  const size_t nparts = bound.size() - 1;
   if (c->gexec_parts.size() < nparts) c->gexec_parts.resize(nparts, nullptr);
   for (size_t k = 0; k < nparts; k++) {
-    const size_t t0 = k * per, t1 = std::min(n, t0 + per);
+    const size_t t0 = bound[k], t1 = bound[k + 1];
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     int rc = enqueue_tasks(c, hs, o, t0, t1, k == 0);
     cudaGraph_t g = nullptr;
