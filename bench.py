@@ -17,6 +17,7 @@ timed region.  The L2 is flushed (256 MB write) before every timed step.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import ctypes as C
 import importlib.util
 import json
@@ -870,6 +871,11 @@ def main():
            "clocks": clk, "gpu_launches": int(launches),
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "candidates_per_step": ncand,
+           # digest of the last step's candidate records and indices: equal
+           # across runs, and across code changes that keep the arithmetic,
+           # for one schedule (the FFT split changes rounding)
+           "candidates_sha1": hashlib.sha1(np.ascontiguousarray(rec).tobytes()
+                                           + np.ascontiguousarray(idx).tobytes()).hexdigest()[:16],
            "schedule": {"spindown_batch": sched[0], "fft_split": sched[1], "lanes": lanes,
                         "autotuned": bool(args.autotune) and not args.schedule}}
 

@@ -536,8 +536,8 @@ template <typename R, int PM> struct SpinLoader {
 //     (mod1) and swaps with its partner lane (lane ^ 1) the term of the array
 //     the partner keeps, so that it holds x_arr = term_0 + term_1: one sincos
 //     per detector and position, as the paired loader.  16-point DFT over a,
-//     twiddle W_256^{b c}, store Z[c][b].
-//   stage 2: warp = column, lane = 2 c + arr.  16-point DFT over b gives
+//     store Z[c][b].
+//   stage 2: warp = column, lane = 2 c + arr.  Twiddle W_256^{b c}, 16-point DFT over b gives
 //     Y[k1 = c + 16 d]; inter-pass twiddle W_L^{n2 k1}; stored like k_pass_a
 //     (the a|b values of one (n2, k1) adjacent, 256 contiguous bytes per warp).
 // Shared tile: Z[c][b][lane] at c * 514 + b * 32 + lane (float2); the pad of
@@ -552,14 +552,24 @@ __global__ void __launch_bounds__(512, 2)
   CtaTrace trace_(KK_SPIN_A);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* z = reinterpret_cast<float2*>(smem_raw);
+  // twiddles of the stage-1 outputs, applied in stage 2: W_256^{b c} at
+  // c * 17 + b (the pitch of 17 makes the stage-2 reads conflict-free)
   float2* tws = z + 16 * ZC;
-  char* lsm = reinterpret_cast<char*>(tws + 256);
+  char* lsm = reinterpret_cast<char*>(tws + 272);
   const int batch = blockIdx.y;
   const int c0 = blockIdx.x << 4;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int m = threadIdx.x; m < 256; m += 512) tws[m] = tw1[m];
-  ld.prologue(batch, lsm);
-  __syncthreads();
+  // loaded now, stored after stage 1: no barrier before the first record
+  // loads (except for the forms whose prologue fills shared memory)
+  float2 twv = make_float2(0.f, 0.f);
+  if (threadIdx.x < 272) {
+    const int tc = threadIdx.x / 17, tb = threadIdx.x - 17 * tc;
+    twv = tw1[tb * tc];
+  }
+  if constexpr (SpinLoader<float, PM>::kPrologue) {
+    ld.prologue(batch, lsm);
+    __syncthreads();
+  }
   const SpinCta pk = ld.consts(batch, lsm);
   float2 v[16];
   {
@@ -578,16 +588,17 @@ __global__ void __launch_bounds__(512, 2)
     }
     dft16<SIGN>(v);
 #pragma unroll
-    for (int c = 1; c < 16; ++c) v[c] = cmul(v[c], tws[w * c]);
-#pragma unroll
     for (int c = 0; c < 16; ++c) z[c * ZC + w * 32 + lane] = v[c];
   }
+  if (threadIdx.x < 272) tws[threadIdx.x] = twv;
   __syncthreads();
   {
     const int arr = lane & 1, c = lane >> 1;
     const int n2 = c0 + w;
+    const float2* t2 = tws + c * 17;
+    v[0] = z[c * ZC + 2 * w + arr];
 #pragma unroll
-    for (int b = 0; b < 16; ++b) v[b] = z[c * ZC + b * 32 + 2 * w + arr];
+    for (int b = 1; b < 16; ++b) v[b] = cmul(z[c * ZC + b * 32 + 2 * w + arr], t2[b]);
     dft16<SIGN>(v);
     float2* yb = ybuf + ((size_t)batch << (LOGL + 1)) + ((size_t)n2 << (LOGL1 + 1)) + arr;
 #pragma unroll
@@ -1196,7 +1207,7 @@ template <typename R, int PM> class EngineT : public Engine {
       // two detectors, L1 = 256: the two-stage radix-16 pass A
       if (ld.nifo == 2 && a16_) {
         auto k16 = k_pass_a16<SIGN, LOGL, IsSpinF32<Loader>::pm>;
-        constexpr int smem16 = (16 * (16 * 32 + 2) + 256) * (int)sizeof(float2) + 128;
+        constexpr int smem16 = (16 * (16 * 32 + 2) + 272) * (int)sizeof(float2) + 128;
         static std::atomic<unsigned long long> done16{0};
         smem_attr(k16, smem16, done16);
         k16<<<ga, 512, smem16, stream>>>(ld, t1, tlo, thi, yb);
