@@ -1076,9 +1076,11 @@ int pa_debug_prelude(pa_ctx* c, int pm, int mm, int nn, double* xa, double* xb, 
   CK(cudaMemcpyAsync(sums, c->b.sums[0], sizeof(sums), cudaMemcpyDeviceToHost, c->stream_pre), "copy");
   CK(cudaStreamSynchronize(c->stream_pre), "prelude");
   const int N = c->sett.N;
+  const int sw = c->eng->swapped_det();
   for (int d = 0; d < c->nifo; d++)
     for (int arr = 0; arr < 2; arr++) {
       double* dst = arr == 0 ? xa : xb;
+      const int half = d == sw ? 1 - arr : arr;  // {xb, xa} records
       if (!dst) continue;
       for (int i = 0; i < N; i++) {
         double re, im;
@@ -1088,7 +1090,7 @@ int pa_debug_prelude(pa_ctx* c, int pm, int mm, int nn, double* xa, double* xb, 
           im = ((double*)buf.data())[2 * src + 1];
         } else {
           // 32-byte records {xa.re, xa.im, xb.re, xb.im | phase terms}
-          const size_t src = 8 * ((size_t)d * N + i) + 2 * arr;
+          const size_t src = 8 * ((size_t)d * N + i) + 2 * half;
           re = ((float*)buf.data())[src];
           im = ((float*)buf.data())[src + 1];
         }

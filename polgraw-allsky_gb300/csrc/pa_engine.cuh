@@ -481,7 +481,9 @@ template <typename R, int PM> struct SpinLoader {
   }
 
   // One detector's term of load2 (FP32 forms, n < N): xm_{a,b,d}[n] times
-  // exp(-i phase_d(n)), with the phase evaluated as load2 does.
+  // exp(-i phase_d(n)), with the phase evaluated as load2 does; pa and pb
+  // follow the record's order (b first for the detector whose record
+  // halves the prelude swapped, Engine::swapped_det).
   __device__ __forceinline__ void mod1(int d, int n, T& pa, T& pb, const SpinCta& pk) const {
     static_assert(sizeof(R) == 4, "FP32 forms only");
     const SpinCta* p = &pk;
@@ -578,10 +580,10 @@ __global__ void __launch_bounds__(512, 2)
 #pragma unroll
     for (int a = 0; a < 16; ++a) {
       const int n = ((16 * a + w) << LOGL2) + n2;
-      float2 pa = make_float2(0.f, 0.f), pb = pa;
-      if (n < ld.N) ld.mod1(arr, n, pa, pb, pk);
-      const float2 send = arr ? pa : pb;
-      const float2 mine = arr ? pb : pa;
+      // detector 1's record holds {xb, xa} (k_splint swap_det): the first
+      // term is the array this lane keeps, the second its partner's
+      float2 mine = make_float2(0.f, 0.f), send = mine;
+      if (n < ld.N) ld.mod1(arr, n, mine, send, pk);
       const float rx = __shfl_xor_sync(0xffffffffu, send.x, 1);
       const float ry = __shfl_xor_sync(0xffffffffu, send.y, 1);
       v[a] = make_float2(mine.x + rx, mine.y + ry);
@@ -923,7 +925,7 @@ template <typename R>
 __global__ void __launch_bounds__(256)
     k_splint(const typename CT<R>::T* __restrict__ y, int ldy, const typename CT<R>::T* __restrict__ y2,
              const double* __restrict__ shftf, const DetConst* __restrict__ dc, int N,
-             typename CT<R>::T* __restrict__ xm) {
+             typename CT<R>::T* __restrict__ xm, int swap_det) {
   typedef typename CT<R>::T T;
   CtaTrace trace_(KK_SPLINT);
   const int d = blockIdx.y;
@@ -953,9 +955,12 @@ __global__ void __launch_bounds__(256)
     xm[((size_t)d * 2 + 0) * N + i] = out[0];
     xm[((size_t)d * 2 + 1) * N + i] = out[1];
   } else {
-    // lower half of the sample's 32-byte record
+    // lower half of the sample's 32-byte record: {xa, xb}, or {xb, xa} for
+    // detector swap_det (the radix-16 spindown pass A then needs no
+    // lane-dependent selects, SpinLoader::mod1r)
+    const int f = d == swap_det ? 1 : 0;
     reinterpret_cast<float4*>(xm)[2 * ((size_t)d * N + i)] =
-        make_float4((float)out[0].x, (float)out[0].y, (float)out[1].x, (float)out[1].y);
+        make_float4((float)out[f].x, (float)out[f].y, (float)out[1 - f].x, (float)out[1 - f].y);
   }
 }
 
@@ -1155,6 +1160,17 @@ template <typename R, int PM> class EngineT : public Engine {
   // (default) or the generic radix-4/8 one (environment PA_SPIN_PASS_A=radix8)
   bool a16_ = true;
 
+  // The spindown pass A is the radix-16 kernel: FP32, two detectors, L1 =
+  // 256 with the current split (the template condition of fft_l).
+  bool use_a16() const {
+    if (sizeof(R) != 4 || b_.nifo != 2 || !a16_) return false;
+    const int m = gm_.logL;
+    return (split_ ? m / 2 : (m + 1) / 2) == 8;
+  }
+  // Detector whose record halves the prelude stores as {xb, xa}: detector 1
+  // when the radix-16 pass A reads the records, else none (-1).
+  int swapped_det() const override { return use_a16() ? 1 : -1; }
+
   // CUDA events around a launch when profiling is on
   void pre(int kind, int items, cudaStream_t st) {
     if (!prof || !prof->on) return;
@@ -1205,7 +1221,7 @@ template <typename R, int PM> class EngineT : public Engine {
     bool done = false;
     if constexpr (IsSpinF32<Loader>::value && G::LOGL1 == 8 && G::C == 16 && NT == 512) {
       // two detectors, L1 = 256: the two-stage radix-16 pass A
-      if (ld.nifo == 2 && a16_) {
+      if (use_a16()) {
         auto k16 = k_pass_a16<SIGN, LOGL, IsSpinF32<Loader>::pm>;
         constexpr int smem16 = (16 * (16 * 32 + 2) + 272) * (int)sizeof(float2) + 128;
         static std::atomic<unsigned long long> done16{0};
@@ -1311,7 +1327,7 @@ template <typename R, int PM> class EngineT : public Engine {
     post(st);
     pre(KK_SPLINT, nifo, st);
     k_splint<R><<<dim3(nbx, nifo), 256, 0, st>>>((const T*)b_.yint, b_.Ninterp, (const T*)b_.y2,
-                                                 b_.shftf, b_.dc, N, (T*)b_.xm[slot]);
+                                                 b_.shftf, b_.dc, N, (T*)b_.xm[slot], swapped_det());
     post(st);
     launches_ += 3;
     return cudaGetLastError();

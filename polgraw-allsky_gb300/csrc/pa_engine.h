@@ -132,6 +132,9 @@ class Engine {
   // odd m only; ignored for even m).
   virtual void set_split(int split) = 0;
   virtual int split() const = 0;
+  // Detector whose 32-byte records (FP32 forms) hold {xb, xa} instead of
+  // {xa, xb}, as the prelude writes them for the current split; -1: none.
+  virtual int swapped_det() const = 0;
   // Per-CTA trace of this engine's kernels into buf (cap records of 48
   // bytes: start/end %globaltimer, start/end clock64, kernel kind, SM id);
   // buf == nullptr switches it off.  trace_count: records written so far
