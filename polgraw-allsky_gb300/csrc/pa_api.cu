@@ -348,6 +348,15 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   if ((rc = make_twiddles(c, s.Ninterp, +1, &c->tw_inv))) return rc;
   if ((rc = make_twiddles(c, s.nfft, +1, &c->tw_invh))) return rc;
   if ((rc = make_twiddles(c, s.nfftf, -1, &c->tw_main))) return rc;
+  if (!c->fp64 && nifo == 2) {  // the radix-16 pass A's twiddles (Engine use_a16)
+    const long L = s.nfftf, n = pa::tw_a16_len(L);
+    std::vector<double> v(2 * (size_t)n);
+    for (long j = 0; j < n; j++) host_twiddle(pa::tw_a16_exp(j, L), L, -1, &v[2 * j], &v[2 * j + 1]);
+    void* p = nullptr;
+    if ((rc = dalloc(c, &p, v.size() * c->rsz))) return rc;
+    if ((rc = upload_real(c, p, v))) return rc;
+    b.tw_a16 = p;
+  }
   for (int k = 0; k < 4; k++) {
     b.tw_fwd[k] = c->tw_fwd.p[k];
     b.tw_inv[k] = c->tw_inv.p[k];
@@ -1224,6 +1233,7 @@ double g_noalloc_tw[2 * (256 + 256 + 1024 + 64)];
 float g_noalloc_tw_f[2 * (256 + 256 + 1024 + 64)];
 float g_noalloc_real[kNoAllocMaxN];
 float g_noalloc_F[kNoAllocMaxNfftf];
+float g_noalloc_tw_a16[2 * kNoAllocMaxNfftf];  // host staging of Buffers::tw_a16
 
 // 256-byte aligned bump layout inside the scratch array
 struct Bump {
@@ -1279,6 +1289,7 @@ size_t noalloc_layout(char* base, const pa_settings& s, int nifo, pa::Buffers* b
   *Fn = m.take(4 * (size_t)bins);  // normalised F (the output)
   b->cand = (pa::DevCand*)m.take(sizeof(pa::DevCand) * kNoAllocCandCap);
   b->ncand = (int*)m.take(16);
+  b->tw_a16 = m.take(cs * (size_t)pa::tw_a16_len(s.nfftf));
   const int lens[4] = {s.nfft, s.Ninterp, s.nfftf, s.nfft};
   for (int t = 0; t < 4; t++) {
     int lg = 0;
@@ -1434,6 +1445,17 @@ extern "C" int pa_fstat_noalloc(const pa_settings* sett, const pa_detector* det,
   NCK(noalloc_twiddles(sett->Ninterp, +1, tw[1], st), "twiddles");
   NCK(noalloc_twiddles(sett->nfftf, -1, tw[2], st), "twiddles");
   NCK(noalloc_twiddles(sett->nfft, +1, tw[3], st), "twiddles");
+  {
+    const long L = sett->nfftf, n = pa::tw_a16_len(L);
+    for (long j = 0; j < n; j++) {
+      double re, im;
+      host_twiddle(pa::tw_a16_exp(j, L), L, -1, &re, &im);
+      g_noalloc_tw_a16[2 * j] = (float)re;
+      g_noalloc_tw_a16[2 * j + 1] = (float)im;
+    }
+    NCK(cudaMemcpyAsync((void*)b.tw_a16, g_noalloc_tw_a16, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, st),
+        "twiddles");
+  }
   // what must start at zero
   NCK(cudaMemsetAsync(b.counter, 0, 16, st), "memset");
   NCK(cudaMemsetAsync(b.ncand, 0, 16, st), "memset");

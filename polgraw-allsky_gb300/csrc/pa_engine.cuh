@@ -540,17 +540,16 @@ template <typename R, int PM> struct SpinLoader {
 //     per detector and position, as the paired loader.  16-point DFT over a,
 //     store Z[c][b].
 //   stage 2: warp = column, lane = 2 c + arr.  Twiddle W_256^{b c}, 16-point DFT over b gives
-//     Y[k1 = c + 16 d]; inter-pass twiddle W_L^{n2 k1}; stored like k_pass_a
+//     Y[k1 = c + 16 d]; inter-pass twiddle W_L^{n2 k1} from a table of all
+//     of them (Buffers::tw_a16, L entries); stored like k_pass_a
 //     (the a|b values of one (n2, k1) adjacent, 256 contiguous bytes per warp).
 // Shared tile: Z[c][b][lane] at c * 514 + b * 32 + lane (float2); the pad of
 // 2 per c makes the stage-2 reads conflict-free (half-warp slots 2c + arr).
 template <int SIGN, int LOGL, int PM>
 __global__ void __launch_bounds__(512, 2)
     k_pass_a16(const __grid_constant__ SpinLoader<float, PM> ld, const float2* __restrict__ tw1,
-               const float2* __restrict__ twlo,
-               const float2* __restrict__ twhi, float2* __restrict__ ybuf) {
+               const float2* __restrict__ tw16, float2* __restrict__ ybuf) {
   constexpr int LOGL1 = 8, LOGL2 = LOGL - LOGL1, ZC = 16 * 32 + 2;
-  constexpr int Lmask = (1 << LOGL) - 1;
   CtaTrace trace_(KK_SPIN_A);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* z = reinterpret_cast<float2*>(smem_raw);
@@ -603,13 +602,12 @@ __global__ void __launch_bounds__(512, 2)
     for (int b = 1; b < 16; ++b) v[b] = cmul(z[c * ZC + b * 32 + 2 * w + arr], t2[b]);
     dft16<SIGN>(v);
     float2* yb = ybuf + ((size_t)batch << (LOGL + 1)) + ((size_t)n2 << (LOGL1 + 1)) + arr;
+    // inter-pass twiddle W_L^{n2 k1}, k1 = c + 16 d, from the table at
+    // [n2][k1] (one load per output instead of two table loads, their
+    // product and the exponent arithmetic)
+    const float2* tw = tw16 + ((size_t)n2 << 8) + c;
 #pragma unroll
-    for (int d = 0; d < 16; ++d) {
-      const int k1 = c + 16 * d;
-      const int m = (n2 * k1) & Lmask;
-      const float2 W = cmul(__ldg(&twlo[m & 1023]), __ldg(&twhi[m >> 10]));
-      yb[2 * k1] = cmul(v[d], W);
-    }
+    for (int d = 0; d < 16; ++d) yb[2 * (c + 16 * d)] = cmul(v[d], __ldg(&tw[16 * d]));
   }
 }
 
@@ -1163,7 +1161,7 @@ template <typename R, int PM> class EngineT : public Engine {
   // The spindown pass A is the radix-16 kernel: FP32, two detectors, L1 =
   // 256 with the current split (the template condition of fft_l).
   bool use_a16() const {
-    if (sizeof(R) != 4 || b_.nifo != 2 || !a16_) return false;
+    if (sizeof(R) != 4 || b_.nifo != 2 || !a16_ || !b_.tw_a16) return false;
     const int m = gm_.logL;
     return (split_ ? m / 2 : (m + 1) / 2) == 8;
   }
@@ -1226,7 +1224,7 @@ template <typename R, int PM> class EngineT : public Engine {
         constexpr int smem16 = (16 * (16 * 32 + 2) + 272) * (int)sizeof(float2) + 128;
         static std::atomic<unsigned long long> done16{0};
         smem_attr(k16, smem16, done16);
-        k16<<<ga, 512, smem16, stream>>>(ld, t1, tlo, thi, yb);
+        k16<<<ga, 512, smem16, stream>>>(ld, t1, (const float2*)b_.tw_a16, yb);
         done = true;
       }
     }

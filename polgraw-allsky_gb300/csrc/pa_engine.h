@@ -6,6 +6,12 @@
 
 namespace pa {
 
+// entries of Buffers::tw_a16 for a main transform of length L
+inline long tw_a16_len(long L) { return L; }
+// exponent m of W_L^m stored at entry j of Buffers::tw_a16: n2 = j / 256,
+// k1 = j % 256
+inline long tw_a16_exp(long j, long L) { return ((j >> 8) * (j & 255)) % L; }
+
 constexpr int kMaxDet = 8;
 
 // Per-context constants of one detector (uploaded once).
@@ -89,6 +95,9 @@ struct Buffers {
   const void* tw_inv[4];            // Ninterp backward (its twlo/twhi give e^{+i pi j/nfft})
   const void* tw_invh[4];           // nfft backward (the half-length resampling transform)
   const void* tw_main[4];           // nfftf forward
+  // FP32 forms: the inter-pass twiddles W_L^{n2 k1} of the radix-16
+  // spindown pass A (L = nfftf, L1 = 256) at [n2][k1], n2 < L/256, k1 < 256
+  const void* tw_a16;
 };
 
 // Kernel kinds for the optional per-launch CUDA-event profile.
