@@ -480,6 +480,24 @@ template <typename R, int PM> struct SpinLoader {
     vb = mk(bccx, bccy);
   }
 
+  // The fixed-point form's term (FP32, n < N) with the high word of H n
+  // given by the caller (hn_hi, carried from position to position): the
+  // phase's high word is the sum of its three terms' high words.  The carries
+  // of the low words that this drops lower it by at most 2 units of 2^-32
+  // turns (3e-9 rad), far below the FP32 rounding of the angle that follows
+  // (up to 2^-25 of a half turn, 9e-8 rad).  pa, pb as in mod1.
+  __device__ __forceinline__ void mod1h(int d, int n, unsigned hn_hi, unsigned ssr, T& pa, T& pb) const {
+    static_assert(sizeof(R) == 4 && PM == PM_FIXED, "fixed-point FP32 form only");
+    const size_t o = (size_t)d * N + n;
+    const float4 lo16 = __ldg(reinterpret_cast<const float4*>(xm) + 2 * o);
+    const uint4 hi16 = __ldg(reinterpret_cast<const uint4*>(xm) + 2 * o + 1);
+    const unsigned th = hi16.y + (__umulhi(hi16.z, ssr) + hi16.w * ssr) + hn_hi;
+    float sn, cs;
+    sincospif((float)(int)th * 4.656612873077393e-10f, &sn, &cs);  // 2^-31
+    pa = mk(lo16.x * cs + lo16.y * sn, lo16.y * cs - lo16.x * sn);
+    pb = mk(lo16.z * cs + lo16.w * sn, lo16.w * cs - lo16.z * sn);
+  }
+
   // One detector's term of load2 (FP32 forms, n < N): xm_{a,b,d}[n] times
   // exp(-i phase_d(n)), with the phase evaluated as load2 does; pa and pb
   // follow the record's order (b first for the detector whose record
@@ -576,13 +594,21 @@ __global__ void __launch_bounds__(512, 2)
   {
     const int arr = lane & 1;
     const int n2 = c0 + (lane >> 1);
+    // fixed-point form: H n carried from position to position (exact, mod 2^64)
+    uint64_t hn = mul64x32(pk.H, (unsigned)((w << LOGL2) + n2));
+    const uint64_t hstep = pk.H << (4 + LOGL2);
 #pragma unroll
     for (int a = 0; a < 16; ++a) {
       const int n = ((16 * a + w) << LOGL2) + n2;
       // detector 1's record holds {xb, xa} (k_splint swap_det): the first
       // term is the array this lane keeps, the second its partner's
       float2 mine = make_float2(0.f, 0.f), send = mine;
-      if (n < ld.N) ld.mod1(arr, n, mine, send, pk);
+      if constexpr (PM == PM_FIXED) {
+        if (n < ld.N) ld.mod1h(arr, n, (unsigned)(hn >> 32), pk.ssr, mine, send);
+        hn += hstep;
+      } else {
+        if (n < ld.N) ld.mod1(arr, n, mine, send, pk);
+      }
       const float rx = __shfl_xor_sync(0xffffffffu, send.x, 1);
       const float ry = __shfl_xor_sync(0xffffffffu, send.y, 1);
       v[a] = make_float2(mine.x + rx, mine.y + ry);
