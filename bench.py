@@ -128,10 +128,10 @@ def l2_flush():
 
 
 # DRAM bytes (read + write) per spindown of the spindown pass A (H1+L1,
-# N=86164, nfftf=131072) from ncu captures of the kernel, per schedule
-# (spindowns per launch, FFT split); scaled by the spindowns of a launch
-PASS_A_TRAFFIC_PER_SPINDOWN = {(32, 0): 13.1e6 / 28.57, (32, 1): 11.49e6 / 32, (64, 1): 79.65e6 / 64,
-                               (64, 0): 77.79e6 / 64}
+# N=86164, nfftf=131072) from an ncu capture of the current kernel, per
+# schedule (spindowns per launch, FFT split); scaled by the spindowns of a
+# launch.  Schedules without a capture of the current kernel report null.
+PASS_A_TRAFFIC_PER_SPINDOWN = {(32, 1): 14.08e6 / 32}
 
 
 def peaks() -> dict:
