@@ -485,7 +485,10 @@ template <typename R, int PM> struct SpinLoader {
   // phase's high word is the sum of its three terms' high words.  The carries
   // of the low words that this drops lower it by at most 2 units of 2^-32
   // turns (3e-9 rad), far below the FP32 rounding of the angle that follows
-  // (up to 2^-25 of a half turn, 9e-8 rad).  pa, pb as in mod1.
+  // (up to 2^-25 of a half turn, 9e-8 rad).  The angle, in [-pi, pi), goes
+  // to the hardware sine and cosine (__sincosf: absolute error at most
+  // 2^-21.41 = 3.6e-7 in that range), which the radix-16 pass A needs once
+  // per detector and sample.  pa, pb as in mod1.
   __device__ __forceinline__ void mod1h(int d, int n, unsigned hn_hi, unsigned ssr, T& pa, T& pb) const {
     static_assert(sizeof(R) == 4 && PM == PM_FIXED, "fixed-point FP32 form only");
     const size_t o = (size_t)d * N + n;
@@ -493,7 +496,7 @@ template <typename R, int PM> struct SpinLoader {
     const uint4 hi16 = __ldg(reinterpret_cast<const uint4*>(xm) + 2 * o + 1);
     const unsigned th = hi16.y + (__umulhi(hi16.z, ssr) + hi16.w * ssr) + hn_hi;
     float sn, cs;
-    sincospif((float)(int)th * 4.656612873077393e-10f, &sn, &cs);  // 2^-31
+    __sincosf((float)(int)th * 1.4629180792671596e-9f, &sn, &cs);  // pi 2^-31
     pa = mk(lo16.x * cs + lo16.y * sn, lo16.y * cs - lo16.x * sn);
     pb = mk(lo16.z * cs + lo16.w * sn, lo16.w * cs - lo16.z * sn);
   }
