@@ -348,14 +348,23 @@ static int build_ctx(pa_ctx* c, const pa_detector* det) {
   if ((rc = make_twiddles(c, s.Ninterp, +1, &c->tw_inv))) return rc;
   if ((rc = make_twiddles(c, s.nfft, +1, &c->tw_invh))) return rc;
   if ((rc = make_twiddles(c, s.nfftf, -1, &c->tw_main))) return rc;
-  if (!c->fp64 && nifo == 2) {  // the radix-16 pass A's twiddles (Engine use_a16)
-    const long L = s.nfftf, n = pa::tw_a16_len(L);
-    std::vector<double> v(2 * (size_t)n);
-    for (long j = 0; j < n; j++) host_twiddle(pa::tw_a16_exp(j, L), L, -1, &v[2 * j], &v[2 * j + 1]);
-    void* p = nullptr;
-    if ((rc = dalloc(c, &p, v.size() * c->rsz))) return rc;
-    if ((rc = upload_real(c, p, v))) return rc;
-    b.tw_a16 = p;
+  if (!c->fp64) {  // inter-pass twiddle tables of the spindown transform, per split
+    const long L = s.nfftf;
+    int lg = 0;
+    while ((1L << lg) < L) ++lg;
+    for (int sp = 0; sp < 2; sp++) {
+      if (sp == 1 && !(lg & 1)) {
+        b.tw_pass[1] = b.tw_pass[0];
+        break;
+      }
+      const int l1 = pa::pass_logl1(lg, sp);
+      std::vector<double> v(2 * (size_t)L);
+      for (long j = 0; j < L; j++) host_twiddle(pa::tw_pass_exp(j, L, l1), L, -1, &v[2 * j], &v[2 * j + 1]);
+      void* p = nullptr;
+      if ((rc = dalloc(c, &p, v.size() * c->rsz))) return rc;
+      if ((rc = upload_real(c, p, v))) return rc;
+      b.tw_pass[sp] = p;
+    }
   }
   for (int k = 0; k < 4; k++) {
     b.tw_fwd[k] = c->tw_fwd.p[k];
@@ -1233,7 +1242,7 @@ double g_noalloc_tw[2 * (256 + 256 + 1024 + 64)];
 float g_noalloc_tw_f[2 * (256 + 256 + 1024 + 64)];
 float g_noalloc_real[kNoAllocMaxN];
 float g_noalloc_F[kNoAllocMaxNfftf];
-float g_noalloc_tw_a16[2 * kNoAllocMaxNfftf];  // host staging of Buffers::tw_a16
+float g_noalloc_tw_pass[2 * kNoAllocMaxNfftf];  // host staging of Buffers::tw_pass
 
 // 256-byte aligned bump layout inside the scratch array
 struct Bump {
@@ -1289,7 +1298,8 @@ size_t noalloc_layout(char* base, const pa_settings& s, int nifo, pa::Buffers* b
   *Fn = m.take(4 * (size_t)bins);  // normalised F (the output)
   b->cand = (pa::DevCand*)m.take(sizeof(pa::DevCand) * kNoAllocCandCap);
   b->ncand = (int*)m.take(16);
-  b->tw_a16 = m.take(cs * (size_t)pa::tw_a16_len(s.nfftf));
+  b->tw_pass[0] = m.take(cs * (size_t)s.nfftf);
+  b->tw_pass[1] = m.take(cs * (size_t)s.nfftf);
   const int lens[4] = {s.nfft, s.Ninterp, s.nfftf, s.nfft};
   for (int t = 0; t < 4; t++) {
     int lg = 0;
@@ -1445,16 +1455,20 @@ extern "C" int pa_fstat_noalloc(const pa_settings* sett, const pa_detector* det,
   NCK(noalloc_twiddles(sett->Ninterp, +1, tw[1], st), "twiddles");
   NCK(noalloc_twiddles(sett->nfftf, -1, tw[2], st), "twiddles");
   NCK(noalloc_twiddles(sett->nfft, +1, tw[3], st), "twiddles");
-  {
-    const long L = sett->nfftf, n = pa::tw_a16_len(L);
-    for (long j = 0; j < n; j++) {
+  for (int sp = 0; sp < 2; sp++) {
+    const long L = sett->nfftf;
+    int lg = 0;
+    while ((1L << lg) < L) ++lg;
+    const int l1 = pa::pass_logl1(lg, sp);
+    for (long j = 0; j < L; j++) {
       double re, im;
-      host_twiddle(pa::tw_a16_exp(j, L), L, -1, &re, &im);
-      g_noalloc_tw_a16[2 * j] = (float)re;
-      g_noalloc_tw_a16[2 * j + 1] = (float)im;
+      host_twiddle(pa::tw_pass_exp(j, L, l1), L, -1, &re, &im);
+      g_noalloc_tw_pass[2 * j] = (float)re;
+      g_noalloc_tw_pass[2 * j + 1] = (float)im;
     }
-    NCK(cudaMemcpyAsync((void*)b.tw_a16, g_noalloc_tw_a16, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, st),
-        "twiddles");
+    NCK(cudaMemcpyAsync((void*)b.tw_pass[sp], g_noalloc_tw_pass, sizeof(float) * 2 * L, cudaMemcpyHostToDevice,
+                        st), "twiddles");
+    NCK(cudaStreamSynchronize(st), "twiddles");  // the staging array is reused
   }
   // what must start at zero
   NCK(cudaMemsetAsync(b.counter, 0, 16, st), "memset");

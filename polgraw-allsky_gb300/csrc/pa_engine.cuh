@@ -261,6 +261,7 @@ template <typename R> struct PlainLoader {
   typedef typename CT<R>::T T;
   static constexpr int kTraceKind = KK_FFT_FWD_A;
   static constexpr bool kEarlyLoads = true;  // no prologue: loads before any barrier
+  static constexpr bool kTwiddleTable = false;
   const T* in;   // [batch][2][ld]
   int len, ld;
   __device__ __forceinline__ void prologue(int, char*) const {}
@@ -288,6 +289,7 @@ template <typename R> struct HalfShiftLoader {
   typedef typename CT<R>::T T;
   static constexpr int kTraceKind = KK_FFT_INV_A;
   static constexpr bool kEarlyLoads = true;  // no prologue: loads before any barrier
+  static constexpr bool kTwiddleTable = false;
   const T* spec;    // [batch][2][nfft]
   const T* twlo;    // e^{+2 pi i m/Ninterp}, m < 1024
   const T* twhi;    // e^{+2 pi i 1024 m/Ninterp}
@@ -352,6 +354,8 @@ template <typename R, int PM> struct SpinLoader {
   static constexpr bool kPrologue = !SpinHet<R, PM>::kHost;
   // generic pass A: first loads before any barrier (no prologue to wait for)
   static constexpr bool kEarlyLoads = !kPrologue;
+  // generic pass A: inter-pass twiddles from Buffers::tw_pass (FP32 forms)
+  static constexpr bool kTwiddleTable = sizeof(R) == 4;
   const T* xm;       // [nifo][2][N]
   const void* ph0;   // FP64 form: tmp1 [nifo][N]; FP32 forms: unused
   int N, nifo, ss0, ss_base, s0_flag;
@@ -397,8 +401,10 @@ template <typename R, int PM> struct SpinLoader {
     const SpinCta* p = &pk;
     R accx = 0, accy = 0, bccx = 0, bccy = 0;
     double base = 0.;
-    uint64_t ibase = 0;
-    if (PM == PM_FIXED) ibase = mul64x32(p->H, (unsigned)n);
+    // fixed-point form: the high word of H n (the phase is formed from the
+    // high words of its terms, as in mod1h)
+    unsigned hn_hi = 0;
+    if (PM == PM_FIXED) hn_hi = __umulhi((unsigned)p->H, (unsigned)n) + (unsigned)(p->H >> 32) * (unsigned)n;
     else if (PM == PM_F64) base = p->het1 * (double)n;
     for (int d = 0; d < nifo; ++d) {
       const size_t o = (size_t)d * N + n;
@@ -434,15 +440,12 @@ template <typename R, int PM> struct SpinLoader {
         sn = (R)sf;
         cs = (R)cf;
       } else if (PM == PM_FIXED) {
-        const uint64_t A = ((uint64_t)hi16.y << 32) | hi16.x;
-        const uint64_t B = ((uint64_t)hi16.w << 32) | hi16.z;
-        const uint64_t t = A + mul64x32(B, p->ssr) + ibase;
-        // top 32 bits as a signed fraction of half a turn: angle = pi * x,
-        // x in [-1, 1) (resolution 2^-31 half-turns = 1.5e-9 rad); the
-        // 32-bit conversion stays off the FP64 pipe
-        const float x = (float)(int)(t >> 32) * 4.656612873077393e-10f;  // 2^-31
+        // top 32 bits of A + B ssr + H n (high words only, as mod1h) as a
+        // signed fraction of half a turn: angle = pi * x, x in [-1, 1); the
+        // hardware sine and cosine (absolute error <= 3.6e-7 there)
+        const unsigned th = hi16.y + (__umulhi(hi16.z, p->ssr) + hi16.w * p->ssr) + hn_hi;
         float sf, cf;
-        sincospif(x, &sf, &cf);
+        __sincosf((float)(int)th * 1.4629180792671596e-9f, &sf, &cf);  // pi 2^-31
         sn = (R)sf;
         cs = (R)cf;
       } else {
@@ -562,7 +565,7 @@ template <typename R, int PM> struct SpinLoader {
 //     store Z[c][b].
 //   stage 2: warp = column, lane = 2 c + arr.  Twiddle W_256^{b c}, 16-point DFT over b gives
 //     Y[k1 = c + 16 d]; inter-pass twiddle W_L^{n2 k1} from a table of all
-//     of them (Buffers::tw_a16, L entries); stored like k_pass_a
+//     of them (Buffers::tw_pass, L entries); stored like k_pass_a
 //     (the a|b values of one (n2, k1) adjacent, 256 contiguous bytes per warp).
 // Shared tile: Z[c][b][lane] at c * 514 + b * 32 + lane (float2); the pad of
 // 2 per c makes the stage-2 reads conflict-free (half-warp slots 2c + arr).
@@ -1190,7 +1193,7 @@ template <typename R, int PM> class EngineT : public Engine {
   // The spindown pass A is the radix-16 kernel: FP32, two detectors, L1 =
   // 256 with the current split (the template condition of fft_l).
   bool use_a16() const {
-    if (sizeof(R) != 4 || b_.nifo != 2 || !a16_ || !b_.tw_a16) return false;
+    if (sizeof(R) != 4 || b_.nifo != 2 || !a16_ || !b_.tw_pass[split_]) return false;
     const int m = gm_.logL;
     return (split_ ? m / 2 : (m + 1) / 2) == 8;
   }
@@ -1253,11 +1256,16 @@ template <typename R, int PM> class EngineT : public Engine {
         constexpr int smem16 = (16 * (16 * 32 + 2) + 272) * (int)sizeof(float2) + 128;
         static std::atomic<unsigned long long> done16{0};
         smem_attr(k16, smem16, done16);
-        k16<<<ga, 512, smem16, stream>>>(ld, t1, (const float2*)b_.tw_a16, yb);
+        k16<<<ga, 512, smem16, stream>>>(ld, t1, (const float2*)b_.tw_pass[SPLIT], yb);
         done = true;
       }
     }
-    if (!done) ka<<<ga, NT, G::smem_a, stream>>>(ld, t1, tlo, thi, yb);
+    const T* twp = nullptr;
+    if constexpr (Loader::kTwiddleTable) {
+      twp = (const T*)b_.tw_pass[SPLIT];
+      if (!twp) return cudaErrorInvalidValue;
+    }
+    if (!done) ka<<<ga, NT, G::smem_a, stream>>>(ld, t1, tlo, thi, twp, yb);
     post(stream);
     pre(kind_b, batch, stream);
     kb<<<gb, NT, G::smem_b, stream>>>(st, t2, yb);

@@ -6,11 +6,14 @@
 
 namespace pa {
 
-// entries of Buffers::tw_a16 for a main transform of length L
-inline long tw_a16_len(long L) { return L; }
-// exponent m of W_L^m stored at entry j of Buffers::tw_a16: n2 = j / 256,
-// k1 = j % 256
-inline long tw_a16_exp(long j, long L) { return ((j >> 8) * (j & 255)) % L; }
+// log2 of the pass-A column length L1 of a length 2^logL transform with
+// factor split `split` (0: L1 = 2^ceil(logL/2); 1, odd logL only: 2^floor)
+inline int pass_logl1(int logL, int split) { return (split && (logL & 1)) ? logL / 2 : (logL + 1) / 2; }
+// exponent m of W_L^m at entry j of Buffers::tw_pass[split]: the inter-pass
+// twiddle W_L^{n2 k1} at (n2 << logL1) + k1
+inline long tw_pass_exp(long j, long L, int logL1) {
+  return ((j >> logL1) * (j & ((1L << logL1) - 1))) % L;
+}
 
 constexpr int kMaxDet = 8;
 
@@ -95,9 +98,10 @@ struct Buffers {
   const void* tw_inv[4];            // Ninterp backward (its twlo/twhi give e^{+i pi j/nfft})
   const void* tw_invh[4];           // nfft backward (the half-length resampling transform)
   const void* tw_main[4];           // nfftf forward
-  // FP32 forms: the inter-pass twiddles W_L^{n2 k1} of the radix-16
-  // spindown pass A (L = nfftf, L1 = 256) at [n2][k1], n2 < L/256, k1 < 256
-  const void* tw_a16;
+  // FP32 forms: the inter-pass twiddles W_L^{n2 k1} of the spindown
+  // transform (L = nfftf) at (n2 << logL1) + k1 for each factor split
+  // (pass_logl1), nfftf entries each; both pointers equal for even log2 L
+  const void* tw_pass[2];
 };
 
 // Kernel kinds for the optional per-launch CUDA-event profile.

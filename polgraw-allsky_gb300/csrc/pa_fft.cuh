@@ -397,13 +397,16 @@ struct CtaTrace {
 // item (blockIdx.y).  The first radix stage takes its inputs from the
 // loader in registers; the last stage (lanes along k1) applies the
 // inter-pass twiddle W_L^{n2 k1} and writes Y[n2][k1][a|b] straight to
-// global memory, 16 contiguous bytes per lane.
+// global memory, 16 contiguous bytes per lane.  The twiddle comes from the
+// table twp of all of them at (n2 << LOGL1) + k1 when the loader's
+// kTwiddleTable is set (the spindown transform of the FP32 forms), else as
+// the product of the two tables twlo, twhi.
 // Loader: prologue(batch, smem scratch) and load2(batch, n, a, b, scratch).
 template <typename R, int SIGN, int LOGL, class Loader, int SPLIT = 0>
 __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
     k_pass_a(const __grid_constant__ Loader ld, const typename CT<R>::T* __restrict__ tw1,
              const typename CT<R>::T* __restrict__ twlo, const typename CT<R>::T* __restrict__ twhi,
-             typename CT<R>::T* __restrict__ ybuf) {
+             const typename CT<R>::T* __restrict__ twp, typename CT<R>::T* __restrict__ ybuf) {
   typedef typename CT<R>::T T;
   typedef FftShape<R, LOGL, SPLIT> G;
   constexpr int E = G::E, NT = G::NT, P = G::PA;
@@ -444,8 +447,13 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int k1 = j + r * Ns;
-      const int m = (n2 * k1) & Lmask;
-      const T W = cmul(__ldg(&twlo[m & 1023]), __ldg(&twhi[m >> 10]));
+      T W;
+      if constexpr (Loader::kTwiddleTable) {
+        W = __ldg(&twp[((size_t)n2 << G::LOGL1) + k1]);
+      } else {
+        const int m = (n2 * k1) & Lmask;
+        W = cmul(__ldg(&twlo[m & 1023]), __ldg(&twhi[m >> 10]));
+      }
       Pair<T>::st(yb + (((size_t)n2 << G::LOGL1) + k1) * 2, cmul(va[r], W), cmul(vb[r], W));
     }
   }
