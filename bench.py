@@ -131,7 +131,7 @@ def l2_flush():
 # N=86164, nfftf=131072) from an ncu capture of the current kernel, per
 # schedule (spindowns per launch, FFT split); scaled by the spindowns of a
 # launch.  Schedules without a capture of the current kernel report null.
-PASS_A_TRAFFIC_PER_SPINDOWN = {(32, 1): 14.08e6 / 32}
+PASS_A_TRAFFIC_PER_SPINDOWN = {(32, 1): 14.21e6 / 32}
 
 
 def peaks() -> dict:
