@@ -659,8 +659,9 @@ template <typename R> struct CStore {
   T* out;   // [batch][2][ldo]
   int ldo;
   R scale;
-  __device__ __forceinline__ void begin(int, int) const {}
-  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, int logL1) const {
+  struct Ctx {};
+  __device__ __forceinline__ Ctx begin() const { return Ctx{}; }
+  __device__ __forceinline__ void put(const Ctx&, int batch, int k1, int k2, T a, T b, int logL1) const {
     const size_t k = (size_t)k1 + ((size_t)k2 << logL1);
     out[((size_t)batch * 2 + 0) * ldo + k] = mk(a.x * scale, a.y * scale);
     out[((size_t)batch * 2 + 1) * ldo + k] = mk(b.x * scale, b.y * scale);
@@ -674,13 +675,16 @@ template <typename R> struct FstatStore {
   R* F;             // [batch][bins]
   const R* inv;     // 1/aa, 1/bb in the working precision
   int nmin, nmax, bins;
-  __device__ __forceinline__ void begin(int, int) const {}
-  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, int logL1) const {
+  // 1/aa and 1/bb, loaded when the CTA starts (beside the first loads of
+  // the intermediate) rather than where the epilogue needs them
+  struct Ctx {
+    R ia, ib;
+  };
+  __device__ __forceinline__ Ctx begin() const { return Ctx{__ldg(&inv[0]), __ldg(&inv[1])}; }
+  __device__ __forceinline__ void put(const Ctx& c, int batch, int k1, int k2, T a, T b, int logL1) const {
     const int k = k1 + (k2 << logL1);
-    if (k >= nmin && k < nmax) {
-      const R ia = __ldg(&inv[0]), ib = __ldg(&inv[1]);
-      F[(size_t)batch * bins + (k - nmin)] = (a.x * a.x + a.y * a.y) * ia + (b.x * b.x + b.y * b.y) * ib;
-    }
+    if (k >= nmin && k < nmax)
+      F[(size_t)batch * bins + (k - nmin)] = (a.x * a.x + a.y * a.y) * c.ia + (b.x * b.x + b.y * b.y) * c.ib;
   }
 };
 
@@ -694,8 +698,9 @@ template <typename R> struct InterpStore {
   const T* xin;     // [batch][2][N]
   int N, Ninterp;
   R scale;          // 1/nfft
-  __device__ __forceinline__ void begin(int, int) const {}
-  __device__ __forceinline__ void put(int batch, int k1, int k2, T a, T b, int logL1) const {
+  struct Ctx {};
+  __device__ __forceinline__ Ctx begin() const { return Ctx{}; }
+  __device__ __forceinline__ void put(const Ctx&, int batch, int k1, int k2, T a, T b, int logL1) const {
     const int m = k1 + (k2 << logL1);
     const size_t qa = (size_t)batch * 2, qb = qa + 1;
     const T xa = m < N ? xin[qa * N + m] : mk((R)0, (R)0);

@@ -463,7 +463,8 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
 // radix stage reads Y[n2][k1][a|b] from global memory (lanes along k1, 16
 // contiguous bytes each); after the last stage every thread hands its
 // outputs X[k1 + L1 k2] for both arrays to the storer:
-//   __device__ void put(int batch, int k1, int k2, T a, T b, int logL1) const
+//   Ctx begin() const   (per-thread constants, loaded when the CTA starts)
+//   __device__ void put(const Ctx&, int batch, int k1, int k2, T a, T b, int logL1) const
 // with consecutive lanes on consecutive k1.
 template <typename R, int SIGN, int LOGL, class Storer, int SPLIT = 0>
 __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
@@ -480,6 +481,7 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
   // last, so their intermediate is the likeliest to be still in L2
   const int batch = gridDim.y - 1 - blockIdx.y;
   const int k10 = blockIdx.x << G::LOGRR;
+  const typename Storer::Ctx sctx = st.begin();
   const T* yb = ybuf + ((size_t)batch << (LOGL + 1));
   // the intermediate is read once, here: evict-first
   auto src = [&](int n2, int rr, T& a, T& b) {
@@ -507,7 +509,7 @@ __global__ void __launch_bounds__(TileCfg<R>::NT, TileCfg<R>::MINB)
     T va[8], vb[8];
     stage_load<SIGN, 8, NT, false, G::LOGL2, G::LOGRR, P, LOGNS>(s, tws, it, j, rr, va, vb);
 #pragma unroll
-    for (int r = 0; r < 8; ++r) st.put(batch, k10 + rr, j + r * Ns, va[r], vb[r], G::LOGL1);
+    for (int r = 0; r < 8; ++r) st.put(sctx, batch, k10 + rr, j + r * Ns, va[r], vb[r], G::LOGL1);
   }
 }
 
