@@ -1090,7 +1090,6 @@ __global__ void __launch_bounds__(256)
   for (int k = 0; k < 16; ++k) {
     const int i = k * 256 + threadIdx.x;
     v[k] *= imu;
-    if (i < cnt) sv[i + 1] = v[k];
     above |= (i < cnt && v[k] > trl) ? (1u << k) : 0u;
   }
   if (Fdbg) {
@@ -1098,6 +1097,14 @@ __global__ void __launch_bounds__(256)
       const int i = k * 256 + threadIdx.x;
       if (i < cnt) Fdbg[(size_t)sidx * bins + base + i] = v[k];
     }
+  }
+  // no bin of the chunk above the threshold (the usual case): no run starts
+  // here (a run from the previous chunk is followed by that chunk's CTA)
+  if (!__syncthreads_or(above != 0u)) return;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int i = k * 256 + threadIdx.x;
+    if (i < cnt) sv[i + 1] = v[k];
   }
   __syncthreads();
   // value of the bin before the chunk, needed only when the chunk's first
