@@ -1003,15 +1003,15 @@ __global__ void __launch_bounds__(256)
 // FStat normalisation and thresholding
 
 // FStat normalisation (auxi.c:214-240) and thresholding (jobcore.c:659-669)
-// in one kernel.  One CTA per 4096-bin chunk of one spindown: it loads the
-// chunk, forms the block mean mu = sum/(2*4096) with a fixed reduction order
-// (16 loads per thread at stride 256, xor tree per warp, warps in order), so a
-// chunk's mu is bit-identical whichever CTA computes it; chunks beyond the
-// last full block stay unnormalised.  Normalised values go to shared memory,
-// where runs of bins above trl are found; a run produces one candidate at
-// its maximum, ties to the later bin.  The neighbour chunks' means are
-// formed on demand (run starting at the chunk's first bin, or reaching its
-// end), with all threads taking part.
+// in one kernel.  One CTA per two 4096-bin chunks of one spindown: it loads
+// the chunks, forms each block mean mu = sum/(2*4096) with a fixed reduction
+// order (16 loads per thread at stride 256, xor tree per warp, warps in
+// order), so a chunk's mu is bit-identical whichever CTA computes it; chunks
+// beyond the last full block stay unnormalised.  When a bin is above trl,
+// the normalised values go to shared memory, where runs of bins above trl
+// are found; a run produces one candidate at its maximum, ties to the later
+// bin.  The neighbour chunks' means are formed on demand (run starting at
+// the chunk's first bin, or reaching its end), with all threads taking part.
 __device__ __forceinline__ void emit_cand(DevCand* cand, int* ncand, int cap, int task, int ss, int ii,
                                           double F) {
   const int slot = atomicAdd(ncand, 1);
@@ -1046,61 +1046,17 @@ template <typename R> __device__ __forceinline__ R chunk_sum(const R* f, int bas
   return sum;
 }
 
+// One chunk's normalised values v (this thread's 16, at k * 256 + tid),
+// loaded as in load_chunk and scaled by its 1/mu: its runs above trl, their
+// candidates, and a run reaching the chunk end followed into the next
+// chunks.  Called by all threads of the CTA (it has barriers).
 template <typename R>
-__global__ void __launch_bounds__(256)
-    k_normthresh(const R* __restrict__ F, int bins, int nblk, int white, R trl, int nmin, int ss0, int task,
-                 DevCand* __restrict__ cand, int* __restrict__ ncand, int cap, R* __restrict__ Fdbg) {
-  __shared__ R sv[4096 + 1];
-  __shared__ R red[8];
-  CtaTrace trace_(KK_THRESHOLD);
-  const int c = blockIdx.x, sidx = blockIdx.y;
+__device__ __forceinline__ void chunk_runs(const R* f, R (&v)[16], unsigned above, int c, int bins, int nblk,
+                                           int white, R trl, int nmin, int ss, int task, DevCand* cand,
+                                           int* ncand, int cap, R* sv, R* red) {
   const int nchunk = (bins + 4095) >> 12;
-  const R* f = F + (size_t)sidx * bins;
   const int base = c * 4096;
   const int cnt = min(4096, bins - base);
-  R v[16];
-  if (cnt == 4096) {
-#pragma unroll
-    for (int k = 0; k < 16; ++k) v[k] = f[base + k * 256 + threadIdx.x];
-  } else {
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const int i = k * 256 + threadIdx.x;
-      v[k] = i < cnt ? f[base + i] : (R)0;
-    }
-  }
-  const bool norm = !white && c < nblk;
-  // normalised value = F * (1/mu), mu = block sum / (2*4096); within one
-  // ulp of F/mu
-  R imu = 1;
-  {
-    R acc = 0;
-#pragma unroll
-    for (int k = 0; k < 16; ++k) acc += v[k];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    R sum = 0;
-    for (int k = 0; k < 8; ++k) sum += red[k];
-    if (norm) imu = (R)(2 * 4096) / sum;
-  }
-  unsigned above = 0;  // bit k: element k*256 + tid is above the threshold
-#pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const int i = k * 256 + threadIdx.x;
-    v[k] *= imu;
-    above |= (i < cnt && v[k] > trl) ? (1u << k) : 0u;
-  }
-  if (Fdbg) {
-    for (int k = 0; k < 16; ++k) {
-      const int i = k * 256 + threadIdx.x;
-      if (i < cnt) Fdbg[(size_t)sidx * bins + base + i] = v[k];
-    }
-  }
-  // no bin of the chunk above the threshold (the usual case): no run starts
-  // here (a run from the previous chunk is followed by that chunk's CTA)
-  if (!__syncthreads_or(above != 0u)) return;
 #pragma unroll
   for (int k = 0; k < 16; ++k) {
     const int i = k * 256 + threadIdx.x;
@@ -1139,7 +1095,7 @@ __global__ void __launch_bounds__(256)
       Fc = Fcb;
       pend = true;
     } else {
-      emit_cand(cand, ncand, cap, task, ss0 + sidx, iib + nmin, Fcb);
+      emit_cand(cand, ncand, cap, task, ss, iib + nmin, Fcb);
     }
   }
   // follow a run across chunk ends; uniform loop, at most one thread active
@@ -1165,7 +1121,88 @@ __global__ void __launch_bounds__(256)
       cont = (j == n2);
     }
   }
-  if (pend) emit_cand(cand, ncand, cap, task, ss0 + sidx, ii + nmin, Fc);
+  if (pend) emit_cand(cand, ncand, cap, task, ss, ii + nmin, Fc);
+  __syncthreads();  // sv is reused by the next chunk
+}
+
+// Two 4096-bin chunks per CTA (blockIdx.x: chunks 2x and 2x + 1 of the
+// spindown blockIdx.y): both chunks' loads in flight together.
+template <typename R>
+__global__ void __launch_bounds__(256)
+    k_normthresh(const R* __restrict__ F, int bins, int nblk, int white, R trl, int nmin, int ss0, int task,
+                 DevCand* __restrict__ cand, int* __restrict__ ncand, int cap, R* __restrict__ Fdbg) {
+  __shared__ R sv[4096 + 1];
+  __shared__ R red[16];
+  CtaTrace trace_(KK_THRESHOLD);
+  const int sidx = blockIdx.y;
+  const int nchunk = (bins + 4095) >> 12;
+  const R* f = F + (size_t)sidx * bins;
+  const int cA = 2 * blockIdx.x, cB = cA + 1;
+  R va[16], vb[16];
+  auto load = [&](int c, R (&v)[16]) {
+    const int base = c * 4096, cnt = c < nchunk ? min(4096, bins - base) : 0;
+    if (cnt == 4096) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) v[k] = f[base + k * 256 + threadIdx.x];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const int i = k * 256 + threadIdx.x;
+        v[k] = i < cnt ? f[base + i] : (R)0;
+      }
+    }
+  };
+  load(cA, va);
+  load(cB, vb);
+  // normalised value = F * (1/mu), mu = block sum / (2*4096); within one
+  // ulp of F/mu.  The two chunks' sums in the same fixed order as one.
+  R accA = 0, accB = 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    accA += va[k];
+    accB += vb[k];
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    accA += __shfl_xor_sync(0xffffffffu, accA, off);
+    accB += __shfl_xor_sync(0xffffffffu, accB, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5] = accA;
+    red[8 + (threadIdx.x >> 5)] = accB;
+  }
+  __syncthreads();
+  R sumA = 0, sumB = 0;
+  for (int k = 0; k < 8; ++k) {
+    sumA += red[k];
+    sumB += red[8 + k];
+  }
+  const R imA = (!white && cA < nblk) ? (R)(2 * 4096) / sumA : (R)1;
+  const R imB = (!white && cB < nblk) ? (R)(2 * 4096) / sumB : (R)1;
+  unsigned abA = 0, abB = 0;  // bit k: element k*256 + tid is above the threshold
+  const int cntA = min(4096, bins - cA * 4096), cntB = cB < nchunk ? min(4096, bins - cB * 4096) : 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int i = k * 256 + threadIdx.x;
+    va[k] *= imA;
+    vb[k] *= imB;
+    abA |= (i < cntA && va[k] > trl) ? (1u << k) : 0u;
+    abB |= (i < cntB && vb[k] > trl) ? (1u << k) : 0u;
+  }
+  if (Fdbg) {
+    for (int k = 0; k < 16; ++k) {
+      const int i = k * 256 + threadIdx.x;
+      if (i < cntA) Fdbg[(size_t)sidx * bins + cA * 4096 + i] = va[k];
+      if (i < cntB) Fdbg[(size_t)sidx * bins + cB * 4096 + i] = vb[k];
+    }
+  }
+  // no bin of either chunk above the threshold (the usual case): no run
+  // starts here (a run from the previous chunk is followed by that chunk's
+  // CTA)
+  if (!__syncthreads_or((abA | abB) != 0u)) return;
+  chunk_runs(f, va, abA, cA, bins, nblk, white, trl, nmin, ss0 + sidx, task, cand, ncand, cap, sv, red);
+  if (cB < nchunk)
+    chunk_runs(f, vb, abB, cB, bins, nblk, white, trl, nmin, ss0 + sidx, task, cand, ncand, cap, sv, red);
 }
 
 // ------------------------------------------------------------------
@@ -1406,7 +1443,7 @@ template <typename R, int PM> class EngineT : public Engine {
     if (e != cudaSuccess) return e;
     const int nchunk = (b_.bins + 4095) / 4096;
     pre(KK_THRESHOLD, nb, st);
-    k_normthresh<R><<<dim3(nchunk, nb), 256, 0, st>>>(Fl, b_.bins, b_.nblk, white, (R)trl,
+    k_normthresh<R><<<dim3((nchunk + 1) / 2, nb), 256, 0, st>>>(Fl, b_.bins, b_.nblk, white, (R)trl,
                                                       b_.nmin, ss0, sky.task, b_.cand, b_.ncand,
                                                       b_.cand_cap, (R*)Fdbg);
     post(st);
