@@ -324,7 +324,14 @@ inline uint64_t het1_turns_fixed(int ss, double M4, double M0) {
   const double x = het1 * kTurnsPerRad64;
   if (!(x > 0.)) return 0;
   if (x >= 18446744073709551616.0) return ~0ull;
-  return (uint64_t)nearbyint(x);
+  // round half to even without depending on the host's rounding mode: below
+  // 2^53, x - floor(x) is exact; from 2^53 on, x is an integer
+  uint64_t r = (uint64_t)x;
+  if (x < 9007199254740992.0) {
+    const double fr = x - (double)r;
+    if (fr > 0.5 || (fr == 0.5 && (r & 1))) ++r;
+  }
+  return r;
 }
 
 // Per-launch spindown constants passed by value with the loader.  The
