@@ -305,6 +305,11 @@ class Context:
             raise SearchError("pa_create failed (%d): %s" % (st.value, self.lib.pa_last_error(None).decode()))
         self.settings = settings
         self.nifo = nifo
+        # search_batch's output buffers, kept from call to call (the library
+        # writes every field of the records and indices it returns)
+        self._out_cap = 0
+        self._out_buf = None
+        self._out_idx = None
 
     def error(self) -> str:
         return self.lib.pa_last_error(self.ctx).decode()
@@ -330,14 +335,19 @@ class Context:
         return buf[:n].copy(), idx_to_array(idx, n), fnum.value
 
     def search_batch(self, tasks, opts: Opts, rng: Range, cap: int = 1 << 18):
-        arr = (Sky * len(tasks))(*[Sky(*t) for t in tasks])
+        # the sky points as the C array of {pm, mm, nn} ints
+        sky = np.ascontiguousarray(np.asarray(tasks, dtype=np.int32).reshape(-1, 3))
+        arr = sky.ctypes.data_as(C.POINTER(Sky))
         sgnlc = C.c_int(0)
         fnum = C.c_int(0)
         needed = C.c_int(0)
         while True:
-            buf = np.zeros((cap, PA_NPAR))
-            idx = (CandIdx * cap)()
-            rc = self.lib.pa_search_batch(self.ctx, arr, len(tasks), C.byref(opts), C.byref(rng),
+            if self._out_cap != cap:
+                self._out_buf = np.empty((cap, PA_NPAR))
+                self._out_idx = (CandIdx * cap)()
+                self._out_cap = cap
+            buf, idx = self._out_buf, self._out_idx
+            rc = self.lib.pa_search_batch(self.ctx, arr, len(sky), C.byref(opts), C.byref(rng),
                                           C.byref(sgnlc), buf.ctypes.data_as(C.POINTER(C.c_double)), cap, idx,
                                           C.byref(fnum), C.byref(needed))
             if rc == PA_ERR_CAPACITY:
