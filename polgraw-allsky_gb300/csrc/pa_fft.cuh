@@ -12,8 +12,10 @@
 // butterflies in registers, data exchanged through shared memory between
 // stages.  The tile layout s[e * Q + q] (element e of sequence q, sequence
 // index fastest) keeps every stage's shared-memory access contiguous across
-// a warp.  The intermediate Y is stored so that each pass-B tile is one
-// contiguous block: ybuf[t][n2][arr][r] with t = k1 / Rr, r = k1 % Rr.
+// a warp.  The intermediate Y is stored as ybuf[batch][n2][k1][arr]: pass A
+// writes the a|b values of one (n2, k1) as one 16-byte pair, consecutive
+// lanes on consecutive k1, and a pass-B tile reads Rr consecutive k1 (Rr x
+// 16 contiguous bytes) at every n2.
 //
 // Loaders (pass A input) and storers (pass B output) are functors, so the
 // phase modulation of the spindown loop, the zero padding, the resampling
