@@ -566,11 +566,14 @@ template <typename R, int PM> struct SpinLoader {
 // between them, each thread holding 16 values of one array.
 //   stage 1: warp w = b (n1 mod 16), lane = 2 col + arr.  At the 16 positions
 //     n1 = 16 a + b of column col the thread evaluates detector arr's term
-//     (mod1) and swaps with its partner lane (lane ^ 1) the term of the array
-//     the partner keeps, so that it holds x_arr = term_0 + term_1: one sincos
-//     per detector and position, as the paired loader.  16-point DFT over a,
-//     store Z[c][b].
-//   stage 2: warp = column, lane = 2 c + arr.  Twiddle W_256^{b c}, 16-point DFT over b gives
+//     (mod1h in the fixed-point form, mod1 in the others) and swaps with its
+//     partner lane (lane ^ 1) the term of the array the partner keeps, so
+//     that it holds x_arr = term_0 + term_1: one sincos per detector and
+//     position, as the paired loader.  Detector 1's records hold {xb, xa}
+//     (k_splint swap_det), so the first term is always the one kept.
+//     16-point DFT over a, store Z[c][b].
+//   stage 2: warp = column, lane = 2 c + arr.  Twiddle W_256^{b c} (shared
+//     table at c * 17 + b, stored after stage 1), 16-point DFT over b gives
 //     Y[k1 = c + 16 d]; inter-pass twiddle W_L^{n2 k1} from a table of all
 //     of them (Buffers::tw_pass, L entries); stored like k_pass_a
 //     (the a|b values of one (n2, k1) adjacent, 256 contiguous bytes per warp).
